@@ -1,0 +1,485 @@
+#!/usr/bin/env python3
+"""Benchmark of the LISA time-domain response + TDI on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload NAME] [--no-cpu-baseline]
+
+One step = one pass of the hot path over one source: the six link
+projections (get_projections) and the TDI channels (get_tdi_delays).  The
+default workload is one galactic binary observed for 1 yr at dt = 5 s
+(6,311,629 samples) with flexing Keplerian orbits, 2nd-generation TDI XYZ and
+Lagrange order 25, all in float64, on the plain FP64 path (bit-identical to the
+reference's CPU arithmetic).
+
+Printed on rank 0, one JSON line:
+  value      output samples/s with the input resident in HBM (device-timed with
+             CUDA events on the launching stream, max over ranks);
+  e2e        the same metric through pyResponseTDI with the input in pinned host
+             memory and X/Y/Z copied back to pinned host memory every step;
+  roofline   the dominant kernel's algorithmic FP64 operations per second
+             against the FP64-pipe peak measured at start-up by the probe
+             kernel (plus its HBM fraction against MEASURED_PEAKS.json);
+  cpu_baseline  the CPU oracle on a bounded slice of the same configuration.
+With --impl reference the CPU implementation is timed instead (all host
+cores, one independent source per process) and printed with "impl":
+"reference".  Under torchrun every rank runs its own source (weak scaling);
+the reference arm runs on rank 0 only.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "lisa-on-gpu_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+YRSID_SI = 31558149.763545603
+T_BUFFER = 1e4
+METRIC = "response+TDI output samples/s"
+UNIT = "samples/s"
+SOURCE = dict(A=1e-22, f=2e-3, fdot=1e-14)
+
+WORKLOADS = {
+    "1yr_dt5_gen2": dict(
+        desc="one galactic binary, 1 yr at dt = 5 s (6,311,629 samples), flexing Keplerian "
+             "orbits (arms +-1 %), 2nd-generation TDI XYZ, Lagrange order 25, float64",
+        dt=5.0, n=int(YRSID_SI / 5.0), orbits="kepler", tdi="2nd generation", order=25),
+    "2p18_dt10_gen1": dict(
+        desc="one galactic binary, 2^18 samples at dt = 10 s, rigid equal-arm orbits, "
+             "1st-generation TDI XYZ, Lagrange order 25, float64",
+        dt=10.0, n=2**18, orbits="equal", tdi="1st generation", order=25),
+}
+DEFAULT_WORKLOAD = "1yr_dt5_gen2"
+CPU_SLICE = 2**16  # samples per source in the CPU measurements
+
+
+# ----------------------------------------------------------------------------- setup
+
+def make_source(w: dict, n: int, seed: int):
+    from fastlisaresponse_gb300 import orbits as om
+    from fastlisaresponse_gb300 import waveforms as wf
+
+    t_max = (math.floor(n * w["dt"] / 1e4) + 3) * 1e4
+    orb = om.KeplerianOrbits(t_max=t_max) if w["orbits"] == "kepler" else \
+        om.EqualArmlengthOrbits(t_max=t_max)
+    rng = np.random.default_rng(seed)
+    iota, phi0, psi = math.acos(rng.uniform(-1, 1)), rng.uniform(0, 2 * math.pi), \
+        rng.uniform(0, math.pi)
+    lam, beta = rng.uniform(0, 2 * math.pi), math.asin(rng.uniform(-1, 1))
+    h = wf.gb_waveform(SOURCE["A"], SOURCE["f"], SOURCE["fdot"], iota, phi0, psi,
+                       np.arange(n) * w["dt"])
+    return orb, np.ascontiguousarray(h), lam, beta
+
+
+def output_samples(n: int, dt: float) -> int:
+    return n - 2 * int(T_BUFFER / dt)
+
+
+# ------------------------------------------------------------------------ CPU side
+
+_worker_state = {}
+
+
+def _cpu_worker_init(wname, n, variant):
+    import oracle
+
+    w = WORKLOADS[wname]
+    orb, h, lam, beta = make_source(w, n, seed=12345)
+    o = oracle.OracleResponseTDI(1.0 / w["dt"], n, orb.pycppdetector_args, orb.x_base,
+                                 order=w["order"], tdi=w["tdi"], variant=variant)
+    _worker_state.update(o=o, h=h, lam=lam, beta=beta)
+
+
+def _cpu_worker_run(_):
+    s = _worker_state
+    t0 = time.perf_counter()
+    s["o"].get_projections(s["h"], s["lam"], s["beta"], t0=0.0, t_buffer=T_BUFFER)
+    s["o"].get_tdi_delays()
+    return time.perf_counter() - t0
+
+
+def cpu_rate(wname: str, cores: int, steps: int, warmup: int, variant: str = "o3"):
+    """Samples/s of the CPU oracle over CPU_SLICE-sample sources of the workload's
+    configuration, `cores` processes each computing its own source per step."""
+    w = WORKLOADS[wname]
+    n = CPU_SLICE
+    per = output_samples(n, w["dt"])
+    ctx = mp.get_context("spawn")
+    walls = []
+    with ctx.Pool(cores, initializer=_cpu_worker_init, initargs=(wname, n, variant)) as pool:
+        for i in range(warmup + steps):
+            t0 = time.perf_counter()
+            pool.map(_cpu_worker_run, range(cores), chunksize=1)
+            if i >= warmup:
+                walls.append(time.perf_counter() - t0)
+    total = sum(walls)
+    return dict(value=per * cores * len(walls) / total, seconds=total,
+                ms_per_step=1e3 * total / len(walls), samples_per_step=per * cores)
+
+
+# ------------------------------------------------------------------------ GPU side
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str):
+        self.gpu_id = gpu_id
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", self.gpu_id], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=5)
+        sms, maxes, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sms.append(float(parts[0]))
+                maxes.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[4:8]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        if not sms:
+            return None
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": max(maxes),
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def measure_fp64_peak(lib, device) -> dict:
+    """FP64 FMA and FP32 FMA rates of this GPU from the probe kernel (best of 3)."""
+    import ctypes
+
+    import torch
+
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    blocks, threads = sms * 8, 256
+    sink = torch.zeros(blocks, dtype=torch.float64, device=device)
+    stream = ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+    out = {}
+    for kind, name, iters in ((0, "fp64_fma", 4000), (1, "fp64_div", 400), (2, "fp32_fma", 40000)):
+        best = None
+        for _ in range(3):
+            ms = ctypes.c_float()
+            rc = lib.flr_probe_pipe_rate(kind, iters, blocks, threads, sink.data_ptr(),
+                                         ctypes.byref(ms), stream)
+            if rc != 0:
+                raise RuntimeError(f"probe kind {kind} failed ({rc})")
+            rate = blocks * threads * iters * 8 / (ms.value * 1e-3)
+            best = rate if best is None else max(best, rate)
+        out[name] = best
+    out["sms"] = sms
+    return out
+
+
+def gpu_uuid(device) -> str:
+    import torch
+
+    props = torch.cuda.get_device_properties(device)
+    uuid = getattr(props, "uuid", None)
+    if uuid is not None:
+        s = str(uuid)
+        return s if s.startswith("GPU-") else "GPU-" + s
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    first = vis.split(",")[device.index] if vis else str(device.index)
+    return first
+
+
+def load_traffic(kernel: str, workload: str):
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as fh:
+        table = json.load(fh)
+    entry = table.get(f"{kernel}@{workload}")
+    return None if entry is None else entry.get("bytes_per_launch")
+
+
+def run_ours(args, rank, world, device):
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+    from fastlisaresponse_gb300 import _lib, perfmodel
+
+    w = WORKLOADS[args.workload]
+    n, dt = w["n"], w["dt"]
+    orb, h, lam, beta = make_source(w, n, seed=1 + rank)
+    resp = flr.pyResponseTDI(1.0 / dt, n, order=w["order"], tdi=w["tdi"], orbits=orb,
+                             force_backend=device)
+    n_out = output_samples(n, dt)
+    h_dev = torch.as_tensor(h, device=device)
+    lib = _lib.lib()
+    peaks = measure_fp64_peak(lib, device)
+
+    # per-kernel CUDA events around the two launches (recorded on the stream the
+    # binding launches on: torch's current stream)
+    ev = {"response": [], "tdi": []}
+    rec = {"on": False}
+
+    def wrap(name, fn):
+        def inner(*a, **k):
+            if not rec["on"]:
+                return fn(*a, **k)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn(*a, **k)
+            e1.record()
+            ev[name].append((e0, e1))
+        return inner
+
+    resp.cpp_response.get_response_wrap = wrap("response", resp.cpp_response.get_response_wrap)
+    resp.cpp_response.get_tdi_delays_wrap = wrap("tdi", resp.cpp_response.get_tdi_delays_wrap)
+
+    def device_step():
+        resp.get_projections(h_dev, lam, beta, t0=0.0, t_buffer=T_BUFFER)
+        resp.get_tdi_delays()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        device_step()
+    torch.cuda.synchronize(device)
+
+    clocks = ClockSampler(gpu_uuid(device))
+    clocks.start()
+    time.sleep(0.4)
+    barrier()
+    torch.cuda.synchronize(device)
+    rec["on"] = True
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(args.steps):
+        device_step()
+    stop.record()
+    torch.cuda.synchronize(device)
+    rec["on"] = False
+    barrier()
+    clock_info = clocks.stop()
+    elapsed = start.elapsed_time(stop) * 1e-3
+    assert resp.status() == 0, flr.describe_status(resp.status())
+
+    # end-to-end: pinned host input -> device -> response + TDI -> pinned host X/Y/Z
+    h_pin = torch.from_numpy(h).pin_memory()
+    out_pin = torch.empty((3, n), dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        resp.get_projections(h_pin, lam, beta, t0=0.0, t_buffer=T_BUFFER)
+        resp.get_tdi_delays()
+        out_pin.copy_(resp.XYZ, non_blocking=True)
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize(device)
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record()
+    torch.cuda.synchronize(device)
+    barrier()
+    e2e_elapsed = e0.elapsed_time(e1) * 1e-3
+
+    # max over ranks
+    times = torch.tensor([elapsed, e2e_elapsed], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
+    elapsed, e2e_elapsed = float(times[0]), float(times[1])
+
+    kern_ms = {k: 1e3 * statistics.mean(a.elapsed_time(b) * 1e-3 for a, b in v)
+               for k, v in ev.items()}
+    tables = resp.tdi_tables_host
+    n_delay_links = int(np.count_nonzero(tables["tdi_link_combinations"] != -11))
+    ops = perfmodel.ops_per_sample(w["order"], tables["num_units"], n_delay_links)
+    computed = {"response": n - 2 * resp.projections_start_ind,
+                "tdi": n - 2 * resp.tdi_start_ind}
+    dominant = max(kern_ms, key=kern_ms.get)
+    launch_ops = ops[dominant] * computed[dominant]
+    achieved = launch_ops / (kern_ms[dominant] * 1e-3)
+    peak = peaks["fp64_fma"]
+    launch_bytes = perfmodel.BYTES_PER_SAMPLE[dominant] * computed[dominant]
+    measured = {}
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as fh:
+            measured = json.load(fh)
+    hbm_peak = measured.get("hbm_gbs")
+    kernel_name = {"response": "response_plain_kernel", "tdi": "tdi_plain_kernel"}[dominant]
+    roofline = {
+        "bound": "fp64",
+        "kernel": kernel_name,
+        "achieved": achieved / 1e9,
+        "peak": peak / 1e9,
+        "unit": "Gop/s",
+        "frac": achieved / peak,
+        "peak_source": "measured in this run: FP64 FMA probe kernel (flr_probe_pipe_rate), "
+                       "best of 3; MEASURED_PEAKS.json has no FP64 figure",
+        "ops_per_sample": ops[dominant],
+        "op_definition": "reference arithmetic, one op per FP64 add/sub/mul/div/sqrt/ceil",
+        "launch_ms": kern_ms[dominant],
+        "algorithmic_bytes": launch_bytes,
+        "traffic": load_traffic(kernel_name, args.workload),
+        "hbm": {"achieved_gbs": launch_bytes / (kern_ms[dominant] * 1e-3) / 1e9,
+                "peak_gbs": hbm_peak,
+                "frac": (launch_bytes / (kern_ms[dominant] * 1e-3) / 1e9 / hbm_peak)
+                if hbm_peak else None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if hbm_peak else None},
+        "kernels_ms": kern_ms,
+        "pipe_peaks_gops": {k: v / 1e9 for k, v in peaks.items() if k != "sms"},
+    }
+    result = {
+        "metric": METRIC,
+        "value": n_out * args.steps * world / elapsed,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * elapsed / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded galactic-binary waveform, analytic orbits)",
+        "config": {"workload": w["desc"], "name": args.workload, "samples_per_step": n_out,
+                   "input_samples": n, "path": "plain FP64 (bit-identical to the reference "
+                   "CPU arithmetic)", "l2": "inputs larger than L2: h 16 B + y_gw 48 B + XYZ "
+                   f"24 B per sample = {88 * n / 1e6:.0f} MB per step"},
+        "e2e": {"value": n_out * args.steps * world / e2e_elapsed, "unit": UNIT,
+                "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 24 * n,
+                "api": "pyResponseTDI.get_projections + get_tdi_delays, pinned host buffers"},
+        "gpu_launches": 2 * args.steps,
+        "roofline": roofline,
+        "clocks": clock_info,
+    }
+    return result
+
+
+def cpu_baseline_line(args, cores: int, variant: str = "o3"):
+    steps = max(1, min(args.steps, 3))
+    r = cpu_rate(args.workload, cores, steps=steps, warmup=1, variant=variant)
+    w = WORKLOADS[args.workload]
+    return {"value": r["value"], "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{cores} independent source(s) of {CPU_SLICE} samples "
+                      f"({output_samples(CPU_SLICE, w['dt'])} output samples each) in the "
+                      f"workload's configuration, {steps} timed passes; C oracle "
+                      f"(oracle/flr_oracle.c, gcc -O3), one process per core",
+            "seconds": r["seconds"]}
+
+
+def run_reference(args):
+    cores = os.cpu_count() or 1
+    w = WORKLOADS[args.workload]
+    r = cpu_rate(args.workload, cores, steps=args.steps, warmup=args.warmup, variant="o3")
+    line = {
+        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded galactic-binary waveform, analytic orbits)",
+        "config": {"workload": w["desc"], "name": args.workload,
+                   "samples_per_step": r["samples_per_step"],
+                   "cpu_slice": f"{CPU_SLICE} samples per source, one source per core"},
+        "impl": "reference",
+        "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cores} sources x {CPU_SLICE} samples per step"},
+        "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "the reference's CPU path, restated in C (oracle/flr_oracle.c) and pinned "
+                "bit for bit to the reference's own compiled CPU code; the port is timed "
+                "because the reference's code cannot be built without its sources and "
+                "lisaanalysistools, which the GPU host does not have",
+    }
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 0)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)), flush=True)
+        return
+
+    # CPU processes are spawned before the first CUDA call
+    cpu_line = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu_line = cpu_baseline_line(args, cores=1)
+
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+
+    flr.build()
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    if world > 1:
+        torch.distributed.init_process_group("nccl", device_id=device)
+    result = run_ours(args, rank, world, device)
+    if cpu_line is not None:
+        result["cpu_baseline"] = cpu_line
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

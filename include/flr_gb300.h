@@ -1,0 +1,178 @@
+/*
+ * flr_gb300.h — C ABI of the GB300 (sm_103a) LISA time-domain response + TDI.
+ *
+ * This is the drop-in boundary for the reference's native layer
+ * (mikekatz04/lisa-on-gpu, package fastlisaresponse).  The reference binds its
+ * CUDA code to Python through pybind11 classes; each entry point below takes
+ * the same arguments, in the same order and with the same meaning, as the
+ * method it replaces, so a backend module can forward calls one to one:
+ *
+ *   OrbitsWrap{CPU,GPU}_responselisa(dt, N, n_arr, ltt_arr, x_arr, links,
+ *       sc_r, sc_e, armlength)      src/fastlisaresponse/cutils/binding_flr.hpp:35-59
+ *                                   -> flr_orbits_create / flr_orbits_destroy
+ *   LISAResponseWrap.get_response_wrap(...)    binding_flr.cxx:38-58,
+ *                                              LISAResponse.cu:674-718
+ *                                   -> flr_get_response
+ *   LISAResponseWrap.get_tdi_delays_wrap(...)  binding_flr.cxx:16-35,
+ *                                              LISAResponse.cu:399-429
+ *                                   -> flr_get_tdi_delays
+ *
+ * Conventions (all entry points):
+ *   - Array arguments are device pointers (cudaMalloc'd, managed, or any
+ *     pointer the GPU can dereference), borrowed for the duration of the call;
+ *     flr_orbits_create also accepts host pointers (it copies the tables).
+ *   - Work is enqueued on `stream` (a cudaStream_t; NULL = legacy default
+ *     stream) and is NOT synchronised: results are ready when the stream is.
+ *     The reference synchronises the whole device after each launch
+ *     (LISAResponse.cu:420,704); call cudaStreamSynchronize for that.
+ *   - Every function returns FLR_OK (0) or a negative FLR_E* code; the text of
+ *     the last error on the calling thread is in flr_last_error().  Argument
+ *     errors are reported before anything is enqueued (the reference's CPU
+ *     binding throws std::invalid_argument -> ValueError for the same cases,
+ *     binding_flr.hpp:66-69).
+ *   - Out-of-range tap reads (a delay window that leaves the input, or an A
+ *     table index outside [0, num_A-2]) are not performed: the kernel records
+ *     FLR_STATUS_* bits in the orbit handle's status word and writes NaN for
+ *     that output sample.  Read the word with flr_orbits_status().
+ *   - Arithmetic: the kernels evaluate the reference's expressions as separately
+ *     rounded IEEE-754 double operations in the reference's order (no fused
+ *     multiply-add, correctly rounded division and square root), so integer
+ *     delay indices and outputs equal those of the reference's CPU path built
+ *     without floating-point contraction, bit for bit.
+ */
+#ifndef FLR_GB300_H
+#define FLR_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FLR_OK 0
+#define FLR_E_INVALID_ARGUMENT (-1)
+#define FLR_E_CUDA (-2)
+#define FLR_E_NO_ORBITS (-3)
+#define FLR_E_UNSUPPORTED (-4)
+
+/* Bits of the per-orbit-handle status word (set by kernels, sticky). */
+#define FLR_STATUS_TAP_OUT_OF_RANGE 0x1u   /* interpolation window left the input   */
+#define FLR_STATUS_A_INDEX_OUT_OF_RANGE 0x2u /* eps/deps outside the A table        */
+#define FLR_STATUS_BAD_LINK 0x4u           /* link number not in the orbit's links  */
+#define FLR_STATUS_BAD_CHANNEL 0x8u        /* TDI channel outside [0,num_channels)  */
+
+/* Largest Lagrange order accepted (h = (order+1)/2 <= 40, the reference's
+ * MAX_ORDER E-table size, LISAResponse.cu:216). */
+#define FLR_MAX_ORDER 79
+
+typedef struct flr_orbits flr_orbits;
+
+/* Version string of this library ("flr_gb300 <semver> sm_103a"). */
+const char *flr_version(void);
+
+/* Text of the last error raised on the calling thread ("" if none). */
+const char *flr_last_error(void);
+
+/*
+ * Upload orbit tables and return a handle (replaces OrbitsWrap*_responselisa,
+ * binding_flr.hpp:35-59).  Layout as lisaanalysistools' pycppdetector_args:
+ *   n_arr  [N][6][3]  link unit vectors (kept for completeness, unused by the
+ *                     response, as in the reference)
+ *   ltt_arr[N][6]     light travel time of each link [s]
+ *   x_arr  [N][3][3]  spacecraft positions [m]
+ *   links  [6]        link numbers (12, 23, 31, 13, 32, 21 by default)
+ *   sc_r   [6], sc_e [6]  receiver / emitter spacecraft of each link (1..3)
+ * on the uniform grid t_k = k*dt, k = 0..N-1 (N >= 2).  Values are linearly
+ * interpolated; times whose segment (int)(t/dt) lies outside [0, N-1] give a
+ * light travel time of 0 and a zero position, the last segment serves t up to
+ * and beyond (N-1)*dt.  Unlike the reference (which borrows the caller's
+ * arrays), the tables are copied into device memory owned by the handle; host
+ * or device pointers are accepted.  The handle also owns the status word.
+ */
+int flr_orbits_create(double dt, int N, const double *n_arr, const double *ltt_arr,
+                      const double *x_arr, const int *links, const int *sc_r, const int *sc_e,
+                      double armlength, flr_orbits **out);
+int flr_orbits_destroy(flr_orbits *orbits);
+
+/* Read (and with reset != 0, clear) the status word; synchronises `stream`. */
+int flr_orbits_status(flr_orbits *orbits, uint32_t *bits, int reset, void *stream);
+
+/*
+ * Link projections y_gw (replaces LISAResponseWrap.get_response_wrap,
+ * binding_flr.cxx:38-58 -> LISAResponse::get_response, LISAResponse.cu:674-718).
+ *   y_gw      [6*num_delays] out, link-major; samples [projections_start_ind,
+ *             num_delays - projections_start_ind) are written, others untouched
+ *   t_data    [num_delays] sample times; t_data[0] is the time origin of input_in
+ *   k_in, u_in, v_in [3] propagation direction and polarisation basis
+ *   dt        sample spacing (unused by the kernel, as in the reference)
+ *   input_in  [num_inputs] complex128 h+ + i hx, interleaved (re, im)
+ *   order     Lagrange order; h = (order+1)/2 taps on each side
+ *   sampling_frequency  1/dt
+ *   buffer_integer      staging margin of the reference's GPU kernel; accepted
+ *                       and ignored (this kernel has no fixed-size window)
+ *   A_in [num_A], deps, E_in [(order+1)/2 - 1]  Lagrange tables (response.py:273-310)
+ */
+int flr_get_response(flr_orbits *orbits, double *y_gw, const double *t_data, const double *k_in,
+                     const double *u_in, const double *v_in, double dt, int num_delays,
+                     const void *input_in, int num_inputs, int order, double sampling_frequency,
+                     int buffer_integer, const double *A_in, double deps, int num_A,
+                     const double *E_in, int projections_start_ind, void *stream);
+
+/*
+ * TDI combinations (replaces LISAResponseWrap.get_tdi_delays_wrap,
+ * binding_flr.cxx:16-35 -> LISAResponse::get_tdi_delays, LISAResponse.cu:399-429).
+ *   delayed_links [num_channels*num_delays] in/out, channel-major; each sample
+ *             in [tdi_start_ind, num_delays - tdi_start_ind) is ACCUMULATED
+ *             into, unit by unit in unit order (callers zero it first, as the
+ *             reference's caller does, response.py:592)
+ *   input_links [6*num_inputs] link streams y_gw, rows in orbit link order
+ *   t_arr     [num_delays] sample times
+ *   unit_starts/unit_lengths [num_units]  slices of tdi_link_combinations
+ *   tdi_base_link [num_units]  link whose stream the unit interpolates
+ *   tdi_link_combinations [...]  link numbers whose L(t) the unit subtracts
+ *                               (-11 = none)
+ *   tdi_signs [num_units] (double), channels [num_units]
+ * Unlike the reference GPU kernel (atomicAdd, LISAResponse.cu:389) the sum over
+ * units is in a fixed order, so results are deterministic.
+ */
+int flr_get_tdi_delays(flr_orbits *orbits, double *delayed_links, const double *input_links,
+                       int num_inputs, int num_delays, const double *t_arr,
+                       const int *unit_starts, const int *unit_lengths, const int *tdi_base_link,
+                       const int *tdi_link_combinations, const double *tdi_signs,
+                       const int *channels, int num_units, int num_channels, int order,
+                       double sampling_frequency, int buffer_integer, const double *A_in,
+                       double deps, int num_A, const double *E_in, int tdi_start_ind,
+                       void *stream);
+
+/*
+ * Diagnostics: the integer delay indices the two kernels above compute, from
+ * the same device code.  d_rec/d_em [6*num_delays] receive, per (link, sample),
+ * ceil((delay - t_data[0]) * fs) - 1 for the receiver and emitter times
+ * (LISAResponse.cu:616-622); d_tdi [num_units*num_delays] the same per (unit,
+ * sample) for the TDI delays (LISAResponse.cu:339-341).  Samples outside the
+ * computed range are untouched.  No counterpart in the reference (its indices
+ * are internal); used to show the indices are bit-exact.
+ */
+int flr_response_delay_indices(flr_orbits *orbits, int *d_rec, int *d_em, const double *t_data,
+                               const double *k_in, int num_delays, double sampling_frequency,
+                               int projections_start_ind, void *stream);
+int flr_tdi_delay_indices(flr_orbits *orbits, int *d_tdi, int num_delays, const double *t_arr,
+                          const int *unit_starts, const int *unit_lengths,
+                          const int *tdi_link_combinations, int num_units,
+                          double sampling_frequency, int tdi_start_ind, void *stream);
+
+/*
+ * Diagnostics: arithmetic-pipe throughput probe (no reference counterpart).
+ * Runs blocks x threads threads, each `iters` iterations of 8 independent
+ * operations of `kind` (0 = FP64 FMA, 1 = FP64 division, 2 = FP32 FMA), timed
+ * with CUDA events on `stream`; synchronises.  Used as the measured FP64-pipe
+ * peak of the roofline.  `sink` is a device buffer of `blocks` doubles.
+ */
+int flr_probe_pipe_rate(int kind, long iters, int blocks, int threads, double *sink,
+                        float *elapsed_ms, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLR_GB300_H */

@@ -1,0 +1,47 @@
+// Internal launch interface between the C ABI (flr_capi.cu) and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "flr_device.cuh"
+
+namespace flr {
+
+struct ResponseArgs {
+    OrbitTables orb;
+    LagrangeTables lt;
+    double *y_gw;            // [6][num_delays]
+    const double *t_data;    // [num_delays]
+    const double *k, *u, *v; // [3] each
+    const double2 *input;    // [num_inputs] complex128
+    long num_delays;
+    long num_inputs;
+    double fs;
+    int start;               // projections_start_ind
+};
+
+struct TdiArgs {
+    OrbitTables orb;
+    LagrangeTables lt;
+    double *out;             // [num_channels][num_delays], accumulated into
+    const double *y;         // [6][num_inputs]
+    long num_inputs;
+    long num_delays;
+    const double *t_arr;     // [num_delays]
+    const int *unit_starts, *unit_lengths, *base_link, *combos, *channels;
+    const double *signs;
+    int num_units;
+    int num_channels;
+    double fs;
+    int start;               // tdi_start_ind
+};
+
+cudaError_t launch_response_plain(const ResponseArgs &a, cudaStream_t stream);
+cudaError_t launch_tdi_plain(const TdiArgs &a, cudaStream_t stream);
+cudaError_t launch_response_indices(const ResponseArgs &a, int *d_rec, int *d_em,
+                                    cudaStream_t stream);
+cudaError_t launch_tdi_indices(const TdiArgs &a, int *d_out, cudaStream_t stream);
+cudaError_t launch_orbit_slopes(const double *tab, double *slope, long n, int stride, double dt,
+                                cudaStream_t stream);
+
+}  // namespace flr

@@ -1,0 +1,222 @@
+// Plain FP64 response and TDI kernels (sm_103a).
+//
+// Compiled with --fmad=false (see flr_device.cuh): these kernels reproduce the
+// reference's CPU arithmetic bit for bit.  Parallel layout:
+//
+//   response: one thread per (sample, link); grid (ceil(n/256), 6).  Each
+//             thread evaluates the geometry of its link at its sample and the
+//             two complex Lagrange interpolations (LISAResponse.cu:431-672).
+//   TDI:      one thread per (sample, channel); grid (ceil(n/256), channels).
+//             The thread walks the units of its channel in unit order and
+//             accumulates into a register, so the sum order is that of the
+//             reference's CPU loop (LISAResponse.cu:300-396) and deterministic
+//             (the reference's GPU kernel uses atomicAdd, LISAResponse.cu:389).
+//
+// Both are FP64-pipe bound: the tap loops issue two IEEE divisions per tap and
+// component.  Inputs are read through the read-only data cache; a block's 256
+// consecutive samples touch a contiguous input window of roughly
+// 256 + 2h + (delay spread) samples, so each tap value is fetched from DRAM
+// once and served from L1/L2 afterwards.
+#include <cuda_runtime.h>
+
+#include "flr_device.cuh"
+#include "flr_internal.h"
+
+namespace flr {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ double quiet_nan() {
+    return __longlong_as_double(0x7ff8000000000000ll);
+}
+
+__global__ void __launch_bounds__(kThreads)
+response_plain_kernel(ResponseArgs a) {
+    const int slot = blockIdx.y;
+    const long i = (long)a.start + (long)blockIdx.x * kThreads + threadIdx.x;
+    if (i >= a.num_delays - a.start) return;
+
+    const double k[3] = {__ldg(a.k), __ldg(a.k + 1), __ldg(a.k + 2)};
+    const double u[3] = {__ldg(a.u), __ldg(a.u + 1), __ldg(a.u + 2)};
+    const double v[3] = {__ldg(a.v), __ldg(a.v + 1), __ldg(a.v + 2)};
+    const double t = __ldg(a.t_data + i);
+    const double t_first = __ldg(a.t_data);
+
+    LinkGeometry g = link_geometry(a.orb, slot, t, t_first, a.fs, k, u, v);
+
+    const int h = a.lt.h;
+    const long lo = (long)min(g.d_rec, g.d_em) - (h - 1);
+    const long hi = (long)max(g.d_rec, g.d_em) + h;
+    double *out = a.y_gw + (size_t)slot * a.num_delays + i;
+    if (lo < 0 || hi >= a.num_inputs) {
+        raise_status(a.orb.status, kStatusTap);
+        *out = quiet_nan();
+        return;
+    }
+    double A_rec, A_em;
+    bool ok = prefactor(a.lt, g.e_rec, A_rec);
+    ok = prefactor(a.lt, g.e_em, A_em) && ok;
+    if (!ok) {
+        raise_status(a.orb.status, kStatusAIndex);
+        *out = quiet_nan();
+        return;
+    }
+    double hp_rec, hc_rec, hp_em, hc_em;
+    lagrange_c128(a.input, g.d_rec, g.e_rec, A_rec, a.lt, hp_rec, hc_rec);
+    lagrange_c128(a.input, g.d_em, g.e_em, A_em, a.lt, hp_em, hc_em);
+
+    double pre = 1. / (1. - g.k_dot_n);
+    double big = (hp_em - hp_rec) * g.xi_p + (hc_em - hc_rec) * g.xi_c;
+    *out = pre * big;
+}
+
+__global__ void __launch_bounds__(kThreads)
+tdi_plain_kernel(TdiArgs a) {
+    const int channel = blockIdx.y;
+    const long i = (long)a.start + (long)blockIdx.x * kThreads + threadIdx.x;
+    if (i >= a.num_delays - a.start) return;
+
+    const double t = __ldg(a.t_arr + i);
+    const double t_first = __ldg(a.t_arr);
+    // L(t) of every link slot; the reference re-evaluates the same
+    // interpolation for each list entry (LISAResponse.cu:331), which yields
+    // these values.
+    double L[kLinks];
+#pragma unroll
+    for (int s = 0; s < kLinks; ++s) L[s] = light_travel_time(a.orb, t, s);
+
+    double *out = a.out + (size_t)channel * a.num_delays + i;
+    double acc = *out;
+    const int h = a.lt.h;
+    for (int unit = 0; unit < a.num_units; ++unit) {
+        const int ch = __ldg(a.channels + unit);
+        if (ch < 0 || ch >= a.num_channels) {
+            raise_status(a.orb.status, kStatusChannel);
+            continue;
+        }
+        if (ch != channel) continue;
+        double delay = t;
+        bool link_ok = true;
+        const int s0 = __ldg(a.unit_starts + unit), n_s = __ldg(a.unit_lengths + unit);
+        for (int s = 0; s < n_s; ++s) {
+            const int link = __ldg(a.combos + s0 + s);
+            if (link == kNoLink) continue;
+            const int slot = link_slot(a.orb, link);
+            if (slot < 0) {
+                link_ok = false;
+                break;
+            }
+            delay -= L[slot];
+        }
+        const int base = link_slot(a.orb, __ldg(a.base_link + unit));
+        if (!link_ok || base < 0) {
+            raise_status(a.orb.status, kStatusLink);
+            acc = quiet_nan();
+            continue;
+        }
+        int d;
+        double eps;
+        split_delay(delay, t_first, a.fs, d, eps);
+        if ((long)d - (h - 1) < 0 || (long)d + h >= a.num_inputs) {
+            raise_status(a.orb.status, kStatusTap);
+            acc = quiet_nan();
+            continue;
+        }
+        double pre;
+        if (!prefactor(a.lt, eps, pre)) {
+            raise_status(a.orb.status, kStatusAIndex);
+            acc = quiet_nan();
+            continue;
+        }
+        double val = lagrange_real(a.y + (size_t)base * a.num_inputs, d, eps, pre, a.lt);
+        val *= __ldg(a.signs + unit);
+        acc += val;
+    }
+    *out = acc;
+}
+
+__global__ void __launch_bounds__(kThreads)
+response_indices_kernel(ResponseArgs a, int *d_rec, int *d_em) {
+    const int slot = blockIdx.y;
+    const long i = (long)a.start + (long)blockIdx.x * kThreads + threadIdx.x;
+    if (i >= a.num_delays - a.start) return;
+    const double k[3] = {__ldg(a.k), __ldg(a.k + 1), __ldg(a.k + 2)};
+    const double zero[3] = {0.0, 0.0, 0.0};
+    LinkGeometry g = link_geometry(a.orb, slot, __ldg(a.t_data + i), __ldg(a.t_data), a.fs, k,
+                                   zero, zero);
+    d_rec[(size_t)slot * a.num_delays + i] = g.d_rec;
+    d_em[(size_t)slot * a.num_delays + i] = g.d_em;
+}
+
+__global__ void __launch_bounds__(kThreads)
+tdi_indices_kernel(TdiArgs a, int *d_out) {
+    const int unit = blockIdx.y;
+    const long i = (long)a.start + (long)blockIdx.x * kThreads + threadIdx.x;
+    if (i >= a.num_delays - a.start) return;
+    const double t = __ldg(a.t_arr + i);
+    double delay = t;
+    const int s0 = __ldg(a.unit_starts + unit), n_s = __ldg(a.unit_lengths + unit);
+    for (int s = 0; s < n_s; ++s) {
+        const int link = __ldg(a.combos + s0 + s);
+        if (link == kNoLink) continue;
+        delay -= light_travel_time(a.orb, t, link_slot(a.orb, link));
+    }
+    int d;
+    double eps;
+    split_delay(delay, __ldg(a.t_arr), a.fs, d, eps);
+    d_out[(size_t)unit * a.num_delays + i] = d;
+}
+
+__global__ void orbit_slopes_kernel(const double *tab, double *slope, long n, int stride,
+                                    double dt) {
+    long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n) return;
+    slope[idx] = (tab[idx + stride] - tab[idx]) / dt;
+}
+
+dim3 sample_grid(long count, int rows) {
+    return dim3((unsigned)((count + kThreads - 1) / kThreads), (unsigned)rows);
+}
+
+}  // namespace
+
+cudaError_t launch_response_plain(const ResponseArgs &a, cudaStream_t stream) {
+    long count = a.num_delays - 2L * a.start;
+    if (count <= 0) return cudaSuccess;
+    response_plain_kernel<<<sample_grid(count, kLinks), kThreads, 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tdi_plain(const TdiArgs &a, cudaStream_t stream) {
+    long count = a.num_delays - 2L * a.start;
+    if (count <= 0 || a.num_channels <= 0) return cudaSuccess;
+    tdi_plain_kernel<<<sample_grid(count, a.num_channels), kThreads, 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_response_indices(const ResponseArgs &a, int *d_rec, int *d_em,
+                                    cudaStream_t stream) {
+    long count = a.num_delays - 2L * a.start;
+    if (count <= 0) return cudaSuccess;
+    response_indices_kernel<<<sample_grid(count, kLinks), kThreads, 0, stream>>>(a, d_rec, d_em);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tdi_indices(const TdiArgs &a, int *d_out, cudaStream_t stream) {
+    long count = a.num_delays - 2L * a.start;
+    if (count <= 0 || a.num_units <= 0) return cudaSuccess;
+    tdi_indices_kernel<<<sample_grid(count, a.num_units), kThreads, 0, stream>>>(a, d_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_orbit_slopes(const double *tab, double *slope, long n, int stride, double dt,
+                                cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    orbit_slopes_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(tab, slope, n, stride,
+                                                                          dt);
+    return cudaGetLastError();
+}
+
+}  // namespace flr

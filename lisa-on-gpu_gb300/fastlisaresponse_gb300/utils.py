@@ -1,0 +1,59 @@
+"""Post-processing helpers of the response path: XYZ -> AET and the overlap
+metric the reference's tests use."""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+try:
+    import torch
+except ImportError:  # pragma: no cover
+    torch = None
+
+
+def AET(X, Y, Z):
+    """A, E, T from X, Y, Z as lisaanalysistools defines them (the reference
+    calls ``lisatools.utils.utility.AET`` at response.py:665):
+    A = (Z - X)/sqrt(2), E = (X - 2Y + Z)/sqrt(6), T = (X + Y + Z)/sqrt(3).
+    Works on numpy arrays and torch tensors alike."""
+    return ((Z - X) / math.sqrt(2.0), (X - 2.0 * Y + Z) / math.sqrt(6.0),
+            (X + Y + Z) / math.sqrt(3.0))
+
+
+def get_overlap(sig1, sig2, phase_maximize=False, use_gpu=False):
+    """Normalised time-domain overlap averaged over channels
+    (``src/fastlisaresponse/utils/utility.py:16-82``).
+
+    ``sig1``/``sig2`` are a list of channels or a single 1-D array (numpy or
+    torch).  Returns the real part of the mean complex overlap, or its modulus
+    with ``phase_maximize``."""
+    def as_list(sig):
+        if isinstance(sig, (list, tuple)):
+            return list(sig)
+        if torch is not None and isinstance(sig, torch.Tensor):
+            return [sig] if sig.ndim < 2 else list(sig)
+        if isinstance(sig, np.ndarray):
+            return [sig] if sig.ndim < 2 else list(sig)
+        raise ValueError("sig1 must be list of or single xp.ndarray.")
+
+    s1, s2 = as_list(sig1), as_list(sig2)
+    assert len(s1) == len(s2)
+    assert len(s1[0]) == len(s2[0])
+    overlap = 0.0 + 0.0j
+    for a, b in zip(s1, s2):
+        if torch is not None and (isinstance(a, torch.Tensor) or isinstance(b, torch.Tensor)):
+            a = torch.as_tensor(a, dtype=torch.float64)
+            b = torch.as_tensor(b, dtype=torch.float64, device=a.device)
+            fa, fb = torch.fft.rfft(a), torch.fft.rfft(b)
+            num = torch.dot(fa.conj(), fb)
+            den = torch.sqrt(torch.dot(fa.conj(), fa) * torch.dot(fb.conj(), fb))
+            overlap += complex((num / den).item())
+        else:
+            fa, fb = np.fft.rfft(np.asarray(a)), np.fft.rfft(np.asarray(b))
+            overlap += np.dot(fa.conj(), fb) / np.sqrt(np.dot(fa.conj(), fa) * np.dot(fb.conj(), fb))
+    overlap /= len(s1)
+    if phase_maximize:
+        return float(abs(overlap))
+    return float(np.real(overlap))

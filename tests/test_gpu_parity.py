@@ -1,0 +1,274 @@
+"""Plain FP64 GPU path vs the reference (golden fixtures) and the CPU oracle.
+
+Tolerance: the spec bar is relative L2 <= 1e-12 per link and per TDI channel
+with integer delay indices bit-exact.  The kernels evaluate the reference's
+expressions in the reference's order without FMA contraction, so the tests
+also assert bit-for-bit equality, which is stronger.
+"""
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import TableOrbits, golden_names, golden_orbit_args, load_golden, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = golden_names()
+REL_L2_TOL = 1e-12
+
+
+def _np(x):
+    return x.detach().cpu().numpy()
+
+
+def _assert_rows(got, want, what):
+    for r in range(want.shape[0]):
+        err = rel_l2(got[r], want[r])
+        assert err <= REL_L2_TOL, f"{what} row {r}: rel L2 {err:.3e}"
+    assert np.array_equal(got, want), f"{what}: not bit-identical"
+
+
+@pytest.mark.parametrize("name", GOLDEN)
+def test_golden_bit_exact(gpu_lib, name):
+    import fastlisaresponse_gb300 as flr
+
+    g = load_golden(name)
+    m = g["meta"]
+    resp = flr.pyResponseTDI(1.0 / m["dt"], m["n"], order=m["order"], tdi=m["tdi"],
+                             orbits=TableOrbits(g), tdi_chan=m["tdi_chan"])
+    resp.get_projections(g["h"], m["lam"], m["beta"], t0=m["t0"], t_buffer=m["t_buffer"])
+    chans = resp.get_tdi_delays()
+    assert resp.tdi_start_ind == int(g["tdi_start_ind"])
+    assert resp.projections_start_ind == int(g["projections_start_ind"])
+    _assert_rows(_np(resp.y_gw), g["y_gw"], "y_gw")
+    _assert_rows(_np(resp.XYZ), g["XYZ"], "XYZ")
+    _assert_rows(np.stack([_np(c) for c in chans]), g["chans"], m["tdi_chan"])
+    assert resp.status() == 0
+
+
+@pytest.mark.parametrize("name", GOLDEN)
+def test_delay_indices_bit_exact(gpu_lib, name):
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+
+    g = load_golden(name)
+    m = g["meta"]
+    n, fs = m["n"], 1.0 / m["dt"]
+    orc = oracle.OracleResponseTDI(fs, n, golden_orbit_args(g), g["x_base"], order=m["order"],
+                                   tdi=m["tdi"])
+    d_rec, d_em = orc.get_projections(g["h"], m["lam"], m["beta"], t0=m["t0"],
+                                      t_buffer=m["t_buffer"], return_indices=True)
+    d_tdi = orc.get_tdi_delays(return_indices=True)
+
+    resp = flr.pyResponseTDI(fs, n, order=m["order"], tdi=m["tdi"], orbits=TableOrbits(g))
+    dev = resp.device
+    k, _, _ = flr.sky_basis(m["lam"], m["beta"])
+    t = torch.as_tensor(m["t0"] + np.arange(n) * (1 / fs), device=dev)
+    ps, ts = orc.projections_start_ind, orc.tdi_start_ind
+    g_rec = torch.full((6 * n,), np.iinfo(np.int32).min, dtype=torch.int32, device=dev)
+    g_em = g_rec.clone()
+    resp.cpp_response.response_delay_indices(g_rec, g_em, t, torch.as_tensor(k, device=dev), n,
+                                             fs, ps)
+    g_tdi = torch.full((resp.num_units * n,), np.iinfo(np.int32).min, dtype=torch.int32,
+                       device=dev)
+    resp.cpp_response.tdi_delay_indices(g_tdi, n, t, resp.unit_starts, resp.unit_lengths,
+                                        resp.tdi_link_combinations, resp.num_units, fs, ts)
+    assert np.array_equal(_np(g_rec), d_rec)
+    assert np.array_equal(_np(g_em), d_em)
+    assert np.array_equal(_np(g_tdi).reshape(resp.num_units, n), d_tdi)
+
+
+def _source(n, dt, seed, f=2e-3, fdot=1e-14, A=1e-22):
+    rng = np.random.default_rng(seed)
+    from fastlisaresponse_gb300 import gb_waveform
+
+    iota, phi0, psi = np.arccos(rng.uniform(-1, 1)), rng.uniform(0, 2 * np.pi), \
+        rng.uniform(0, np.pi)
+    lam, beta = rng.uniform(0, 2 * np.pi), np.arcsin(rng.uniform(-1, 1))
+    h = gb_waveform(A, f, fdot, iota, phi0, psi, np.arange(n) * dt)
+    return h, lam, beta
+
+
+def test_plain_config_small_source_full_oracle(gpu_lib):
+    """2^18 samples at dt = 10 s, rigid equal-arm orbits, order 25, 1st-gen
+    XYZ: every sample against the oracle."""
+    import fastlisaresponse_gb300 as flr
+
+    n, dt = 2**18, 10.0
+    orb = flr.EqualArmlengthOrbits(t_max=(n * dt // 1e4 + 3) * 1e4)
+    h, lam, beta = _source(n, dt, seed=0)
+    resp = flr.pyResponseTDI(1 / dt, n, order=25, tdi="1st generation", orbits=orb)
+    resp.get_projections(h, lam, beta, t0=0.0, t_buffer=1e4)
+    X, Y, Z = resp.get_tdi_delays()
+    orc = oracle.OracleResponseTDI(1 / dt, n, orb.pycppdetector_args, orb.x_base, order=25,
+                                   tdi="1st generation")
+    orc.get_projections(h, lam, beta, t0=0.0, t_buffer=1e4)
+    Xo, Yo, Zo = orc.get_tdi_delays()
+    _assert_rows(_np(resp.y_gw), orc.y_gw, "y_gw")
+    _assert_rows(np.stack([_np(X), _np(Y), _np(Z)]), np.stack([Xo, Yo, Zo]), "XYZ")
+    assert resp.status() == 0
+
+
+def test_one_year_gen2_windows_and_properties(gpu_lib):
+    """1 yr at dt = 5 s (6.3e6 samples), flexing Keplerian orbits, 2nd-gen
+    TDI: oracle on windows at the start, middle and end; full-size properties
+    (finite, zero outside the valid range, deterministic)."""
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+
+    dt = 5.0
+    n = int(flr.orbits.YRSID_SI / dt)
+    orb = flr.KeplerianOrbits(t_max=(n * dt // 1e4 + 3) * 1e4)
+    h, lam, beta = _source(n, dt, seed=1)
+    resp = flr.pyResponseTDI(1 / dt, n, order=25, tdi="2nd generation", orbits=orb)
+    resp.get_projections(h, lam, beta, t0=0.0, t_buffer=1e4)
+    resp.get_tdi_delays()
+    y = _np(resp.y_gw)
+    xyz = _np(resp.XYZ)
+    ps, ts = resp.projections_start_ind, resp.tdi_start_ind
+    assert np.all(np.isfinite(y)) and np.all(np.isfinite(xyz))
+    assert np.all(y[:, :ps] == 0) and np.all(y[:, n - ps:] == 0)
+    assert np.all(xyz[:, :ts] == 0) and np.all(xyz[:, n - ts:] == 0)
+    assert np.count_nonzero(xyz[:, ts:n - ts]) == 3 * (n - 2 * ts)
+
+    o = oracle.OracleResponseTDI(1 / dt, n, orb.pycppdetector_args, orb.x_base, order=25,
+                                 tdi="2nd generation")
+    k, u, v = oracle.sky_basis(lam, beta)
+    t = np.arange(n) * o.dt
+    tb = o.tables
+    for i0 in (ts, n // 2 - 2048, n - ts - 4096):
+        win = (i0, i0 + 4096)
+        y_o = np.zeros(6 * n)
+        oracle.get_response(o.orbits, y_o, t, k, u, v, n, h, 25, 1 / dt, o.A_in, o.deps, o.E_in,
+                            ps, sample_range=win)
+        _assert_rows(y[:, win[0]:win[1]], y_o.reshape(6, n)[:, win[0]:win[1]],
+                     f"y_gw window {win}")
+        x_o = np.zeros(3 * n)
+        oracle.get_tdi_delays(o.orbits, x_o, y.reshape(-1), n, n, t, tb["unit_starts"],
+                              tb["unit_lengths"], tb["tdi_base_links"],
+                              tb["tdi_link_combinations"], tb["tdi_signs"], tb["channels"],
+                              tb["num_units"], 25, 1 / dt, o.A_in, o.deps, o.E_in, ts,
+                              sample_range=win)
+        x_o = x_o.reshape(3, n)
+        _assert_rows(xyz[:, win[0]:win[1]], x_o[:, win[0]:win[1]], f"XYZ window {win}")
+
+    first = resp.XYZ.clone()
+    resp.get_projections(h, lam, beta, t0=0.0, t_buffer=1e4)
+    resp.get_tdi_delays()
+    assert torch.equal(first, resp.XYZ)
+    assert resp.status() == 0
+
+
+def test_side_stream_and_device_inputs(gpu_lib):
+    """Device-resident torch inputs on a non-default stream give the same bits."""
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+
+    g = load_golden(GOLDEN[0])
+    m = g["meta"]
+    resp = flr.pyResponseTDI(1.0 / m["dt"], m["n"], order=m["order"], tdi=m["tdi"],
+                             orbits=TableOrbits(g))
+    h = torch.as_tensor(g["h"], device=resp.device)
+    s = torch.cuda.Stream(device=resp.device)
+    with torch.cuda.stream(s):
+        resp.get_projections(h, m["lam"], m["beta"], t0=m["t0"], t_buffer=m["t_buffer"])
+        resp.get_tdi_delays()
+    s.synchronize()
+    assert np.array_equal(_np(resp.y_gw), g["y_gw"])
+    assert np.array_equal(_np(resp.XYZ), g["XYZ"])
+
+
+def test_response_wrapper_reference_test_setup(gpu_lib):
+    """ResponseWrapper as the reference's test builds it (GBWave, AET,
+    remove_garbage), on a short observation, against the oracle chain."""
+    import fastlisaresponse_gb300 as flr
+
+    dt = 10.0
+    n = 8192
+    T = n * dt / flr.orbits.YRSID_SI
+    orb = flr.KeplerianOrbits(t_max=(n * dt // 1e4 + 3) * 1e4)
+    params = (1.084702251e-22, 2.35962078e-3, 1.47197271e-17, 1.11820901, 4.91128699, 2.3290324)
+    lam, beta = 5.22979888, 0.9805742971871619
+    h_host = flr.GBWave()(*params, T=T, dt=dt)[:n]
+
+    orc = oracle.OracleResponseTDI(1 / dt, n, orb.pycppdetector_args, orb.x_base, order=25,
+                                   tdi="1st generation", tdi_chan="AET")
+    orc.get_projections(h_host, lam, beta, t0=0.0, t_buffer=1e4)
+    want = np.stack(orc.get_tdi_delays())[:, 1000:-1000]
+
+    def host_waveform(*args, T=1.0, dt=10.0):
+        return h_host
+
+    kw = dict(t_buffer=1e4, remove_sky_coords=True, is_ecliptic_latitude=True,
+              remove_garbage=True, n_overide=n, orbits=orb, order=25, tdi="1st generation",
+              tdi_chan="AET")
+    chans = flr.ResponseWrapper(host_waveform, T, dt, 6, 7, **kw)(*params, lam, beta)
+    assert len(chans) == 3 and all(len(c) == n - 2000 for c in chans)
+    _assert_rows(np.stack([_np(c) for c in chans]), want, "AET")
+
+    # waveform generated by torch on the GPU: its cos/sin differ from numpy's
+    # in the last bits, so the reference test's own criterion applies
+    def device_waveform(*args, T=1.0, dt=10.0):
+        return flr.GBWave(device="cuda")(*args, T=T, dt=dt)[:n]
+
+    chans = flr.ResponseWrapper(device_waveform, T, dt, 6, 7, **kw)(*params, lam, beta)
+    got = np.stack([_np(c) for c in chans])
+    assert abs(1.0 - flr.get_overlap(list(got), list(want))) < 1e-10
+
+
+def test_kernel_bounds_checks_flag_bad_windows(gpu_lib):
+    """A start index of 0 makes the first samples' interpolation windows reach
+    before the input; the kernel skips those reads, writes NaN there and sets
+    the status bit instead of reading out of bounds."""
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+
+    g = load_golden(GOLDEN[0])
+    m = g["meta"]
+    n = m["n"]
+    resp = flr.pyResponseTDI(1.0 / m["dt"], n, order=m["order"], tdi=m["tdi"],
+                             orbits=TableOrbits(g))
+    dev = resp.device
+    k, u, v = (torch.as_tensor(a, device=dev) for a in flr.sky_basis(m["lam"], m["beta"]))
+    t = torch.as_tensor(m["t0"] + np.arange(n) * resp.dt, device=dev)
+    h = torch.as_tensor(g["h"], device=dev)
+    y = torch.zeros(6 * n, dtype=torch.float64, device=dev)
+    assert resp.status(reset=True) == 0
+    resp.cpp_response.get_response_wrap(y, t, k, u, v, resp.dt, n, h, n, m["order"],
+                                        1 / resp.dt, resp.buffer_integer, resp.A_in, resp.deps,
+                                        len(resp.A_in), resp.E_in, 0)
+    bits = resp.status(reset=True)
+    assert bits & 0x1
+    y = _np(y).reshape(6, n)
+    assert np.isnan(y[:, 0]).all()
+    ps = int(g["projections_start_ind"])
+    assert np.array_equal(y[:, ps:n - ps], g["y_gw"][:, ps:n - ps])
+    assert resp.status() == 0
+
+
+def test_argument_errors_raise(gpu_lib):
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+
+    g = load_golden(GOLDEN[0])
+    m = g["meta"]
+    resp = flr.pyResponseTDI(1.0 / m["dt"], m["n"], order=m["order"], tdi=m["tdi"],
+                             orbits=TableOrbits(g))
+    dev = resp.device
+    y_bad = torch.zeros(6 * m["n"] - 1, dtype=torch.float64, device=dev)
+    t = torch.zeros(m["n"], dtype=torch.float64, device=dev)
+    k = torch.zeros(3, dtype=torch.float64, device=dev)
+    h = torch.zeros(m["n"], dtype=torch.complex128, device=dev)
+    with pytest.raises(ValueError, match="y_gw: input arrays have the incorrect length"):
+        resp.cpp_response.get_response_wrap(y_bad, t, k, k, k, 10.0, m["n"], h, m["n"], 25, 0.1,
+                                            51, resp.A_in, resp.deps, 1001, resp.E_in, 780)
+    y = torch.zeros(6 * m["n"], dtype=torch.float64, device=dev)
+    with pytest.raises(ValueError, match="order"):
+        resp.cpp_response.get_response_wrap(y, t, k, k, k, 10.0, m["n"], h, m["n"], 0, 0.1, 51,
+                                            resp.A_in, resp.deps, 1001, resp.E_in, 780)
