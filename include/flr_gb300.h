@@ -121,7 +121,8 @@ int flr_get_response(flr_orbits *orbits, double *y_gw, const double *t_data, con
 /*
  * TDI combinations (replaces LISAResponseWrap.get_tdi_delays_wrap,
  * binding_flr.cxx:16-35 -> LISAResponse::get_tdi_delays, LISAResponse.cu:399-429).
- *   delayed_links [num_channels*num_delays] in/out, channel-major; each sample
+ *   delayed_links [num_channels*num_delays] in/out, channel-major (it must
+ *             hold num_channels rows: every row is read and written); each sample
  *             in [tdi_start_ind, num_delays - tdi_start_ind) is ACCUMULATED
  *             into, unit by unit in unit order (callers zero it first, as the
  *             reference's caller does, response.py:592)
@@ -132,6 +133,9 @@ int flr_get_response(flr_orbits *orbits, double *y_gw, const double *t_data, con
  *   tdi_link_combinations [...]  link numbers whose L(t) the unit subtracts
  *                               (-11 = none)
  *   tdi_signs [num_units] (double), channels [num_units]
+ *   The caller guarantees unit_starts[u] + unit_lengths[u] <= the length of
+ *   tdi_link_combinations (the kernel cannot check it: the array's length is
+ *   not an argument, as in the reference).
  * Unlike the reference GPU kernel (atomicAdd, LISAResponse.cu:389) the sum over
  * units is in a fixed order, so results are deterministic.
  */

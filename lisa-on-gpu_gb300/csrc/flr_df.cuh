@@ -1,0 +1,130 @@
+// Double-float ("df") arithmetic: a value is the unevaluated sum hi + lo of
+// two FP32 numbers, giving about 48 significand bits on the FP32 pipe (which
+// on GB300 issues ~70x more operations per clock than the FP64 pipe).
+//
+// Built from the classical error-free transformations:
+//   TwoSum (Knuth, TAOCP vol. 2, 4.2.2): s + e = a + b exactly, 6 flops;
+//   FastTwoSum (Dekker 1971): the same in 3 flops when |a| >= |b|;
+//   TwoProduct with FMA: p + e = a * b exactly, 2 flops;
+// and the compensated dot product of Ogita, Rump and Oishi ("Accurate sum and
+// dot product", SIAM J. Sci. Comput. 26, 2005), Dot2: products split exactly,
+// high parts summed with TwoSum, all error terms gathered in a float.
+//
+// Translation units using this header are compiled with --fmad=false, so the
+// compiler cannot fuse the separate multiplies and adds these algorithms rely
+// on; every FMA below is explicit.
+#pragma once
+
+namespace flr {
+namespace df {
+
+struct f2 {
+    float hi, lo;
+};
+
+__device__ __forceinline__ f2 two_sum(float a, float b) {
+    float s = a + b;
+    float bb = s - a;
+    float e = (a - (s - bb)) + (b - bb);
+    return {s, e};
+}
+
+// Requires |a| >= |b| (or a == 0).
+__device__ __forceinline__ f2 fast_two_sum(float a, float b) {
+    float s = a + b;
+    float e = b - (s - a);
+    return {s, e};
+}
+
+__device__ __forceinline__ f2 two_prod(float a, float b) {
+    float p = a * b;
+    return {p, __fmaf_rn(a, b, -p)};
+}
+
+// Split an FP64 value into hi + lo (|lo| <= ulp(hi)/2; exact to ~2^-48).
+__device__ __forceinline__ f2 from_double(double x) {
+    float hi = __double2float_rn(x);
+    float lo = __double2float_rn(x - (double)hi);
+    return {hi, lo};
+}
+
+__device__ __forceinline__ double to_double(f2 a) { return (double)a.hi + (double)a.lo; }
+
+__device__ __forceinline__ f2 renorm(f2 a) { return fast_two_sum(a.hi, a.lo); }
+
+// a + b, result normalised.
+__device__ __forceinline__ f2 add(f2 a, f2 b) {
+    f2 s = two_sum(a.hi, b.hi);
+    return fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
+}
+
+// a - b, result normalised.
+__device__ __forceinline__ f2 sub(f2 a, f2 b) {
+    f2 s = two_sum(a.hi, -b.hi);
+    return fast_two_sum(s.hi, s.lo + (a.lo - b.lo));
+}
+
+// a * b with the lo*lo term dropped (relative error ~2^-46); not normalised
+// (|lo| is a few ulp of hi at most), which the consumers below accept.
+__device__ __forceinline__ f2 mul_raw(f2 a, f2 b) {
+    f2 p = two_prod(a.hi, b.hi);
+    p.lo = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, p.lo));
+    return p;
+}
+
+__device__ __forceinline__ f2 mul(f2 a, f2 b) { return renorm(mul_raw(a, b)); }
+
+// float + df, for |j| >= |a| (the Lagrange denominators j + eps, j >= 1).
+__device__ __forceinline__ f2 add_big_float(float j, f2 a) {
+    f2 s = fast_two_sum(j, a.hi);
+    s.lo += a.lo;
+    return s;
+}
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// 1 / b for b in [1, 64): hardware approximation refined by one Newton step
+// carried out on the df residual, r = r0 + r0 * (1 - b r0); relative error
+// about 1e-14.  Not normalised.
+__device__ __forceinline__ f2 rcp(f2 b) {
+    float r0 = rcp_approx(b.hi);
+    float t = __fmaf_rn(-b.hi, r0, 1.0f);
+    t = __fmaf_rn(-b.lo, r0, t);
+    return {r0, r0 * t};
+}
+
+// Dot2 accumulator (Ogita-Rump-Oishi): sum of df products.
+struct Acc {
+    float s;    // running FP32 sum of the high parts
+    float c;    // gathered error terms and low parts
+};
+
+__device__ __forceinline__ void acc_init(Acc &a) {
+    a.s = 0.f;
+    a.c = 0.f;
+}
+
+// a += w * x for df w and df x.
+__device__ __forceinline__ void acc_fma(Acc &a, f2 w, f2 x) {
+    f2 p = two_prod(w.hi, x.hi);
+    float cross = __fmaf_rn(w.hi, x.lo, __fmaf_rn(w.lo, x.hi, p.lo));
+    f2 s = two_sum(a.s, p.hi);
+    a.s = s.hi;
+    a.c += s.lo + cross;
+}
+
+// a += v for a df value v.
+__device__ __forceinline__ void acc_add(Acc &a, f2 v) {
+    f2 s = two_sum(a.s, v.hi);
+    a.s = s.hi;
+    a.c += s.lo + v.lo;
+}
+
+__device__ __forceinline__ f2 acc_value(const Acc &a) { return fast_two_sum(a.s, a.c); }
+
+}  // namespace df
+}  // namespace flr

@@ -7,7 +7,7 @@
 // fraction of the response kernels has a measured denominator.
 //
 //   kind 0: FP64 fused multiply-add  (8 independent chains per thread)
-//   kind 1: FP64 correctly rounded division (8 independent chains)
+//   kind 1: FP64 correctly rounded division (8 independent chains, x <- a/x)
 //   kind 2: FP32 fused multiply-add  (8 independent chains)
 //
 // Every thread runs `iters` iterations of 8 operations; the chains are folded
@@ -39,7 +39,7 @@ __global__ void probe_ddiv(long iters, double a, double b, double *sink) {
     for (int c = 0; c < 8; ++c) x[c] = threadIdx.x * 1e-3 + c + 1.0;
     for (long it = 0; it < iters; ++it) {
 #pragma unroll
-        for (int c = 0; c < 8; ++c) x[c] = a / x[c] + b;
+        for (int c = 0; c < 8; ++c) x[c] = a / x[c];
     }
     double s = 0.0;
 #pragma unroll
@@ -79,7 +79,7 @@ extern "C" int flr_probe_pipe_rate(int kind, long iters, int blocks, int threads
     if (kind == 0)
         probe_dfma<<<blocks, threads, 0, s>>>(iters, 0.999999, 1e-7, sink);
     else if (kind == 1)
-        probe_ddiv<<<blocks, threads, 0, s>>>(iters, 0.75, 0.5, sink);
+        probe_ddiv<<<blocks, threads, 0, s>>>(iters, 0.75, 0.0, sink);
     else
         probe_ffma<<<blocks, threads, 0, s>>>(iters, 0.999999f, 1e-7f, sink);
     cudaEventRecord(e1, s);

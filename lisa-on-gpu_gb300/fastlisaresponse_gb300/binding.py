@@ -175,6 +175,28 @@ class LISAResponseWrap:
         if not isinstance(orbits, OrbitsWrap):
             raise TypeError("orbits must be an OrbitsWrap")
         self.orbits = orbits
+        self._checked_units = {}
+
+    def _check_unit_tables(self, us, ul, bl, lc, sg, ch, num_units, num_channels):
+        """The kernel follows unit_starts/unit_lengths into
+        tdi_link_combinations and writes the rows named by `channels`; check
+        once per set of table arrays that they stay inside their arrays (the
+        reference checks neither)."""
+        key = tuple((a.ptr, a.size, getattr(a.obj, "_version", None)) for a in
+                    (us, ul, bl, lc, sg, ch)) + (num_units, num_channels)
+        if key in self._checked_units:
+            return
+        starts = _host_copy(us.obj).astype(np.int64)[:num_units]
+        lengths = _host_copy(ul.obj).astype(np.int64)[:num_units]
+        chans = _host_copy(ch.obj)[:num_units]
+        if num_units and (starts.min() < 0 or lengths.min() < 0 or
+                          (starts + lengths).max() > lc.size):
+            raise ValueError("unit_starts/unit_lengths point outside tdi_link_combinations")
+        if num_units and (chans.min() < 0 or chans.max() >= num_channels):
+            raise ValueError("channels must lie in [0, num_channels)")
+        if len(self._checked_units) > 64:
+            self._checked_units.clear()
+        self._checked_units[key] = True
 
     def get_response_wrap(self, y_gw, t_data, k_in, u_in, v_in, dt, num_delays, input_in,
                           num_inputs, order, sampling_frequency, buffer_integer, A_in, deps,
@@ -214,6 +236,8 @@ class LISAResponseWrap:
         ch = _Array(channels, np.int32, "channels").check_min(num_units)
         A = _Array(A_in, np.float64, "A_in").check_length(num_A, 1)
         E = _Array(E_in, np.float64, "E_in").check_min(max(int((order + 1) / 2) - 1, 0))
+        out.check_min(int(num_channels) * num_delays)
+        self._check_unit_tables(us, ul, bl, lc, sg, ch, num_units, int(num_channels))
         rc = _lib.lib().flr_get_tdi_delays(
             self.orbits.handle, out.ptr, y.ptr, num_inputs, num_delays, t.ptr, us.ptr, ul.ptr,
             bl.ptr, lc.ptr, sg.ptr, ch.ptr, num_units, int(num_channels), int(order),
@@ -239,6 +263,10 @@ class LISAResponseWrap:
         us = _Array(unit_starts, np.int32, "unit_starts").check_length(int(num_units), 1)
         ul = _Array(unit_lengths, np.int32, "unit_lengths").check_length(int(num_units), 1)
         lc = _Array(tdi_link_combinations, np.int32, "tdi_link_combinations")
+        starts, lengths = _host_copy(us.obj).astype(np.int64), _host_copy(ul.obj).astype(np.int64)
+        if int(num_units) and (starts.min() < 0 or lengths.min() < 0 or
+                               (starts + lengths).max() > lc.size):
+            raise ValueError("unit_starts/unit_lengths point outside tdi_link_combinations")
         _lib.check(_lib.lib().flr_tdi_delay_indices(
             self.orbits.handle, d.ptr, int(num_delays), t.ptr, us.ptr, ul.ptr, lc.ptr,
             int(num_units), float(sampling_frequency), int(tdi_start_ind), _stream_for(d)))

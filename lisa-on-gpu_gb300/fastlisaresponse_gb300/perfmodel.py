@@ -3,9 +3,15 @@
 Used for the roofline figures of the benchmark.  Counts follow the
 reference's arithmetic (``LISAResponse.cu:110-207`` interpolation,
 ``:559-668`` link geometry, ``:300-396`` TDI; orbit interpolation as restated
-from lisaanalysistools): every FP64 add, subtract, multiply, divide, square
-root and ceil is one operation; each is counted once per output even where the
-reference evaluates the same value again (the TDI light travel times).
+from lisaanalysistools) with per-knot constants (the segment slopes) hoisted
+and identical subexpressions counted once.  FP64 operations are split into
+divide-class operations (division, square root), which the FP64 pipe executes
+as multi-instruction sequences, and the rest (add, subtract, multiply, ceil,
+conversions), one pipe slot each.
+
+The roofline of the plain path is the FP64 pipe: ``slots = ops + divs * c``
+with ``c`` the measured FMA-slots per division (probe kernel), against the
+measured FP64 FMA peak.
 
 Bytes are the compulsory DRAM traffic of the two-kernel path: the complex
 input read once (16 B), the six link streams written and read once (48 B each
@@ -16,37 +22,49 @@ excluded (they are tiny or computable).
 from __future__ import annotations
 
 
-def response_ops_per_link_sample(h: int) -> int:
-    """FP64 ops of one (link, sample) projection with h = (order+1)//2."""
-    ltt = 1 + 6             # segment t/dt, lerp (hi-lo, /dt, dt*w, t-, *, +)
-    x_rec = 1 + 3 * 6       # one segment, three coordinates
-    x_em = 1 + 1 + 3 * 6    # t - L, segment, three coordinates
-    unit_vector = 3 + 3 + 3 + 1 + 3   # differences, squares, sums, sqrt, divisions
-    xi = 6 + 6 + 4 + 1      # u.n, v.n, xi_plus, xi_cross
-    dots = 3 * 6            # k.n, k.x_rec, k.x_em
-    delays = 2 * 2          # k.x * C_inv, t - ...
-    splits = 2 * 6          # (d - t0), *fs, ceil, 1+d, *fs, -
-    prefactors = 2 * 8      # eps/deps, ind*deps, -, /deps, 1-frac, 2 mul, add
-    interp = 15 + 13 * (h - 1)   # complex: B, D, per tap pair (F, G, 4 div, 2 add,
-    #                              2 mul, 2 acc), final 6 per component
-    output = 8              # 1 - k.n, reciprocal, 2 sub, 2 mul, add, mul
-    return ltt + x_rec + x_em + unit_vector + xi + dots + delays + splits + prefactors + \
-        2 * interp + output
+def response_counts(h: int) -> dict:
+    """FP64 ops and divide-class ops of one (link, sample) projection."""
+    ops = (4          # L(t): t - dt*w, slope*(.) + lo           (+1 div: segment)
+           + 6        # x_rec(t): 3 coordinates, shares (t - dt*w)
+           + 1 + 8    # t_em = t - L; x_em(t_em)                 (+1 div: segment)
+           + 9        # n = x_rec - x_em, |n|^2                  (+1 sqrt, +3 div)
+           + 17       # u.n, v.n, xi_plus, xi_cross
+           + 18       # k.n, k.x_rec, k.x_em
+           + 4        # delays t - k.x * C_inv
+           + 2 * 6    # index splits: -t0, *fs, ceil, cvt, 1+d, -
+           + 2 * 6    # A(eps) lerp: cvt, ind*deps, -, 1-frac, 2 mul + add  (+2 div each)
+           + 2 * (14 + 8 * (h - 1))   # complex interp: B, D, F, G, 2 adds, 2 mul E,
+           #                            2 acc per tap pair; 6 per component at the end
+           + 7)       # 1 - k.n, 2 sub, 2 mul, add, mul          (+1 div)
+    divs = 1 + 1 + 4 + 2 * 2 + 2 * 4 * (h - 1) + 1
+    return {"ops": ops, "divs": divs}
 
 
-def tdi_ops_per_sample(h: int, num_units: int, num_delay_links: int) -> int:
-    """FP64 ops of all TDI units of one sample; num_delay_links counts the
-    link entries that subtract a light travel time (the -11 markers excluded)."""
-    ltt = 1 + 6 * 6          # L(t) of the six links (one shared segment)
-    per_unit = 6 + 8 + (9 + 8 * (h - 1)) + 2   # split, prefactor, real interp, sign, add
-    return ltt + num_units * per_unit + num_delay_links
+def tdi_counts(h: int, num_units: int, num_delay_links: int) -> dict:
+    """FP64 ops and divide-class ops of all TDI units of one sample;
+    num_delay_links counts the link entries that subtract a light travel time
+    (the -11 markers excluded)."""
+    ops = (2 + 6 * 2                              # L(t) of the six links (+1 div)
+           + num_delay_links                      # delay -= L
+           + num_units * (6 + 6 + 8 + 5 * (h - 1) + 2))
+    #       split, A lerp, real interp (B, D, final 6; F, G, add, mul E, acc per tap
+    #       pair), sign and accumulate
+    divs = 1 + num_units * (2 + 2 * (h - 1))
+    return {"ops": ops, "divs": divs}
 
 
-def ops_per_sample(order: int, num_units: int, num_delay_links: int) -> dict:
+def counts_per_sample(order: int, num_units: int, num_delay_links: int) -> dict:
     h = (order + 1) // 2
-    resp = 6 * response_ops_per_link_sample(h)
-    tdi = tdi_ops_per_sample(h, num_units, num_delay_links)
-    return {"response": resp, "tdi": tdi, "total": resp + tdi}
+    r = response_counts(h)
+    t = tdi_counts(h, num_units, num_delay_links)
+    return {"response": {"ops": 6 * r["ops"], "divs": 6 * r["divs"]},
+            "tdi": t,
+            "total": {"ops": 6 * r["ops"] + t["ops"], "divs": 6 * r["divs"] + t["divs"]}}
+
+
+def fp64_slots(counts: dict, div_cost: float) -> float:
+    """FP64-pipe FMA slots of `counts` with a division costing `div_cost` slots."""
+    return counts["ops"] + counts["divs"] * div_cost
 
 
 BYTES_PER_SAMPLE = {

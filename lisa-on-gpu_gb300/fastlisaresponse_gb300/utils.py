@@ -17,7 +17,16 @@ def AET(X, Y, Z):
     """A, E, T from X, Y, Z as lisaanalysistools defines them (the reference
     calls ``lisatools.utils.utility.AET`` at response.py:665):
     A = (Z - X)/sqrt(2), E = (X - 2Y + Z)/sqrt(6), T = (X + Y + Z)/sqrt(3).
-    Works on numpy arrays and torch tensors alike."""
+
+    Works on numpy arrays and torch tensors.  For CUDA tensors the constants
+    are 0-d device tensors: torch divides by a host scalar as a multiplication
+    by its reciprocal, which is not the correctly rounded quotient numpy
+    computes."""
+    if torch is not None and isinstance(X, torch.Tensor) and X.is_cuda:
+        def c(v):
+            return torch.tensor(v, dtype=X.dtype, device=X.device)
+        two, r2, r6, r3 = c(2.0), c(math.sqrt(2.0)), c(math.sqrt(6.0)), c(math.sqrt(3.0))
+        return ((Z - X) / r2, (X - two * Y + Z) / r6, (X + Y + Z) / r3)
     return ((Z - X) / math.sqrt(2.0), (X - 2.0 * Y + Z) / math.sqrt(6.0),
             (X + Y + Z) / math.sqrt(3.0))
 
