@@ -166,6 +166,35 @@ int flr_tdi_delay_indices(flr_orbits *orbits, int *d_tdi, int num_delays, const 
                           double sampling_frequency, int tdi_start_ind, void *stream);
 
 /*
+ * Link projections without any device allocation.  No counterpart in the
+ * reference: for callers that cannot call cudaMalloc -- code running inside a
+ * framework that has pre-allocated the GPU's memory, and samplers that must
+ * not trigger the device-wide synchronisation of cudaMalloc/cudaFree in their
+ * inner loop.  Same arguments and
+ * results (bit for bit) as flr_get_response, except that the orbit tables are
+ * passed directly instead of through an flr_orbits handle:
+ *   orbit_dt, orbit_N       grid spacing and knot count, orbit_N <= FLR_NOALLOC_MAX_KNOTS
+ *   ltt_arr [orbit_N][6], x_arr [orbit_N][3][3]   device pointers
+ *   links, sc_r, sc_e [6]   HOST arrays (read during the call)
+ * The derived segment slopes and the status word live in a fixed array inside
+ * the library (3.9 MB of device memory on every GPU that loads it, held until
+ * exit), rewritten and cleared by every call.  The first call on a device,
+ * with that device current, looks up the array's device address; make it
+ * before any stream capture.  Calls whose work can overlap on the GPU race on
+ * the array.  Sizes beyond the limit return FLR_E_INVALID_ARGUMENT with the
+ * reason in flr_last_error().
+ */
+#define FLR_NOALLOC_MAX_KNOTS 32768
+int flr_get_response_noalloc(double orbit_dt, int orbit_N, const double *ltt_arr,
+                             const double *x_arr, const int *links, const int *sc_r,
+                             const int *sc_e, double *y_gw, const double *t_data,
+                             const double *k_in, const double *u_in, const double *v_in,
+                             double dt, int num_delays, const void *input_in, int num_inputs,
+                             int order, double sampling_frequency, int buffer_integer,
+                             const double *A_in, double deps, int num_A, const double *E_in,
+                             int projections_start_ind, void *stream);
+
+/*
  * Diagnostics: arithmetic-pipe throughput probe (no reference counterpart).
  * Runs blocks x threads threads, each `iters` iterations of 8 independent
  * operations of `kind` (0 = FP64 FMA, 1 = FP64 division, 2 = FP32 FMA), timed

@@ -91,6 +91,8 @@ int check_lagrange(int order, const double *A, double deps, int num_A, const dou
 
 }  // namespace
 
+void flr::set_last_error(const std::string &msg) { g_last_error = msg; }
+
 extern "C" {
 
 const char *flr_version(void) { return "flr_gb300 0.1.0 sm_103a"; }

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "flr_device.cuh"
 
 namespace flr {
@@ -41,6 +43,9 @@ cudaError_t launch_tdi_plain(const TdiArgs &a, cudaStream_t stream);
 cudaError_t launch_response_indices(const ResponseArgs &a, int *d_rec, int *d_em,
                                     cudaStream_t stream);
 cudaError_t launch_tdi_indices(const TdiArgs &a, int *d_out, cudaStream_t stream);
+// Sets the text flr_last_error() returns on the calling thread.
+void set_last_error(const std::string &msg);
+
 cudaError_t launch_orbit_slopes(const double *tab, double *slope, long n, int stride, double dt,
                                 cudaStream_t stream);
 

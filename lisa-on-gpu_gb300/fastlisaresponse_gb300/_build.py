@@ -30,6 +30,7 @@ SOURCES = {
     "flr_plain.cu": ["--fmad=false"],
     "flr_capi.cu": [],
     "flr_probe.cu": [],
+    "flr_noalloc.cu": ["--fmad=false"],
 }
 
 _lock = threading.Lock()
