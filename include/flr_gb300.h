@@ -166,6 +166,77 @@ int flr_tdi_delay_indices(flr_orbits *orbits, int *d_tdi, int num_delays, const 
                           double sampling_frequency, int tdi_start_ind, void *stream);
 
 /*
+ * ------------------------------------------------------------------------
+ * Batched, fused response + TDI (no reference counterpart: the reference
+ * evaluates one source per call, with two launches and a device
+ * synchronisation each, LISAResponse.cu:399-429, 674-718).  One persistent
+ * kernel evaluates many sources of different lengths; the link streams stay
+ * in shared memory, so per output sample only the complex input is read and
+ * the three channels are written.
+ *
+ * Arithmetic (per plan):
+ *   FLR_PRECISION_FP64   every operation as in the plain path: outputs are
+ *                        bit-identical to flr_get_response + flr_get_tdi_delays
+ *                        (+ the XYZ->AET transform) on the same inputs;
+ *   FLR_PRECISION_MIXED  delays, their integer/fractional split, orbit
+ *                        interpolation and TDI delay sums in FP64 (integer
+ *                        indices bit-exact), Lagrange taps, weights and
+ *                        projections in double-float (pairs of FP32) arithmetic.
+ * ------------------------------------------------------------------------
+ */
+#define FLR_PRECISION_FP64 0
+#define FLR_PRECISION_MIXED 1
+#define FLR_CHAN_XYZ 0
+#define FLR_CHAN_AET 1 /* lisaanalysistools AET: (Z-X)/sqrt2, (X-2Y+Z)/sqrt6, (X+Y+Z)/sqrt3 */
+#define FLR_CHAN_AE 2
+
+/* One TDI combination, in the reference's table layout (response.py:372-433,
+ * 619-633); HOST arrays, read at plan creation. */
+typedef struct {
+    int num_units;
+    const int *unit_starts;           /* [num_units] */
+    const int *unit_lengths;          /* [num_units] */
+    const int *tdi_base_link;         /* [num_units] link numbers */
+    const int *tdi_link_combinations; /* [num_combos] link numbers, -11 = no delay */
+    const double *tdi_signs;          /* [num_units] */
+    const int *channels;              /* [num_units] 0, 1, 2 */
+    int num_combos;
+} flr_tdi_units;
+
+/* One source of a batch. */
+typedef struct {
+    const void *h;          /* [n] complex128 h+ + i hx, device, 16-byte aligned */
+    double *out;            /* [3][n] float64, device: rows X,Y,Z (or A,E,T / A,E);
+                               samples [tdi_start, n - tdi_start) are written, the
+                               rest untouched (zero it to match the reference) */
+    long long n;
+    int projections_start;  /* link streams are zero outside [ps, n - ps) */
+    int tdi_start;          /* first output sample (garbage margin) */
+    double t0;              /* time of sample 0; sample i is at t0 + i * (1/fs) */
+    double k[3], u[3], v[3];/* propagation direction and polarisation basis */
+    int tdi_set;            /* index of the plan's TDI unit set */
+    int reserved;
+} flr_batch_source;
+
+typedef struct flr_batch_plan flr_batch_plan;
+
+/* Plan for batches on `orbits`: Lagrange tables (device or host; copied),
+ * 1..64 TDI unit sets, precision, tile = output samples per work item
+ * (0 = 512).  Runs of one plan must be ordered on one stream. */
+int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, double deps,
+                          int num_A, const double *E_in, double sampling_frequency,
+                          const flr_tdi_units *sets, int num_sets, int precision, int tile,
+                          flr_batch_plan **out);
+int flr_batch_plan_destroy(flr_batch_plan *plan);
+/* info[0..6] = tile, y halo, input window capacity, link row capacity, shared
+ * memory bytes per block, persistent grid size, precision. */
+int flr_batch_plan_info(const flr_batch_plan *plan, int *info, int n_info);
+
+/* Evaluate `num_sources` sources (host array of descriptors) on `stream`. */
+int flr_batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int num_sources,
+                  int chan, void *stream);
+
+/*
  * Link projections without any device allocation.  No counterpart in the
  * reference: for callers that cannot call cudaMalloc -- code running inside a
  * framework that has pre-allocated the GPU's memory, and samplers that must

@@ -1,0 +1,374 @@
+// C ABI of the batched path: plans and runs of the fused response + TDI
+// kernel over many sources (declarations in include/flr_gb300.h).
+//
+// A plan fixes what is common to a batch -- orbit tables, Lagrange order and
+// tables, TDI unit sets, arithmetic, tile length -- derives the launch shape
+// (halo and window sizes, shared memory, persistent grid from the occupancy of
+// the kernel), and owns reusable device and pinned buffers for the per-run
+// source descriptors and work list.  A run flattens its sources into
+// (source, tile) work items, copies descriptors and items with one
+// asynchronous copy each, and launches one persistent kernel on the stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/flr_gb300.h"
+#include "flr_fused.h"
+#include "flr_internal.h"
+
+struct flr_batch_plan {
+    int device;
+    bool mixed;
+    flr::FusedArgs base;
+    size_t smem;
+    int grid_max;
+    int num_sets;
+    int set_max_len;           // longest TDI delay list (links subtracted)
+    void *d_tables;            // A, E and the TDI sets (device)
+    flr::FusedSource *d_sources;
+    size_t cap_sources;
+    int2 *d_work;
+    size_t cap_work;
+    unsigned char *h_stage;    // pinned staging for descriptors and work items
+    size_t cap_stage;
+    cudaEvent_t stage_free;    // recorded after the staging copies of the last run
+    bool stage_pending;
+};
+
+namespace {
+
+int fail(int code, const std::string &msg) {
+    flr::set_last_error(msg);
+    return code;
+}
+
+int cuda_fail(cudaError_t err, const std::string &what) {
+    return fail(FLR_E_CUDA, what + ": " + cudaGetErrorString(err));
+}
+
+int current_device_is(int dev) {
+    int cur = -1;
+    cudaError_t err = cudaGetDevice(&cur);
+    if (err != cudaSuccess) return cuda_fail(err, "cudaGetDevice");
+    if (cur != dev)
+        return fail(FLR_E_INVALID_ARGUMENT, "plan was created on device " + std::to_string(dev) +
+                                                " but device " + std::to_string(cur) +
+                                                " is current");
+    return FLR_OK;
+}
+
+int slot_of(const flr_orbits *o, int link) {
+    for (int s = 0; s < 6; ++s)
+        if (o->links[s] == link) return s;
+    return -1;
+}
+
+void release(flr_batch_plan *p) {
+    if (!p) return;
+    if (p->d_tables) cudaFree(p->d_tables);
+    if (p->d_sources) cudaFree(p->d_sources);
+    if (p->d_work) cudaFree(p->d_work);
+    if (p->h_stage) cudaFreeHost(p->h_stage);
+    if (p->stage_free) cudaEventDestroy(p->stage_free);
+    delete p;
+}
+
+}  // namespace
+
+extern "C" {
+
+int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, double deps,
+                          int num_A, const double *E_in, double sampling_frequency,
+                          const flr_tdi_units *sets, int num_sets, int precision, int tile,
+                          flr_batch_plan **out) {
+    flr::set_last_error("");
+    if (!out) return fail(FLR_E_INVALID_ARGUMENT, "out must not be NULL");
+    *out = nullptr;
+    if (!orbits) return fail(FLR_E_NO_ORBITS, "Must add orbits with add_orbit_information method.");
+    int rc = current_device_is(orbits->device);
+    if (rc) return rc;
+    const int h = (order + 1) / 2;
+    if (order < 1 || h > flr::kFusedMaxH)
+        return fail(FLR_E_INVALID_ARGUMENT, "order must be in [1, " +
+                                                std::to_string(2 * flr::kFusedMaxH - 1) + "]");
+    if (!A_in || num_A < 2 || !(deps > 0.0) || (h > 1 && !E_in))
+        return fail(FLR_E_INVALID_ARGUMENT, "invalid Lagrange tables");
+    if (!(sampling_frequency > 0.0))
+        return fail(FLR_E_INVALID_ARGUMENT, "sampling_frequency must be positive");
+    if (!sets || num_sets < 1 || num_sets > 64)
+        return fail(FLR_E_INVALID_ARGUMENT, "need 1..64 TDI unit sets");
+    if (precision != FLR_PRECISION_FP64 && precision != FLR_PRECISION_MIXED)
+        return fail(FLR_E_INVALID_ARGUMENT, "precision must be FLR_PRECISION_FP64 or _MIXED");
+    if (tile == 0) tile = 512;
+    if (tile < 32 || tile > 8192) return fail(FLR_E_INVALID_ARGUMENT, "tile must be in [32, 8192]");
+
+    // TDI sets: map link numbers to slots, check sizes
+    std::vector<flr::FusedTdiSet> hsets(num_sets);
+    int max_len = 0;
+    for (int si = 0; si < num_sets; ++si) {
+        const flr_tdi_units &in = sets[si];
+        flr::FusedTdiSet &s = hsets[si];
+        std::memset(&s, 0, sizeof(s));
+        if (in.num_units < 1 || in.num_units > flr::kFusedMaxUnits || in.num_combos < 0 ||
+            in.num_combos > flr::kFusedMaxCombos || !in.unit_starts || !in.unit_lengths ||
+            !in.tdi_base_link || !in.tdi_link_combinations || !in.tdi_signs || !in.channels)
+            return fail(FLR_E_INVALID_ARGUMENT,
+                        "TDI set " + std::to_string(si) + ": 1.." +
+                            std::to_string(flr::kFusedMaxUnits) + " units and at most " +
+                            std::to_string(flr::kFusedMaxCombos) + " link entries");
+        s.num_units = in.num_units;
+        s.num_combos = in.num_combos;
+        for (int c = 0; c < in.num_combos; ++c) {
+            const int link = in.tdi_link_combinations[c];
+            s.combo_slot[c] = (link == -11) ? -1 : slot_of(orbits, link);
+            if (link != -11 && s.combo_slot[c] < 0)
+                return fail(FLR_E_INVALID_ARGUMENT,
+                            "TDI link " + std::to_string(link) + " is not an orbit link");
+        }
+        for (int u = 0; u < in.num_units; ++u) {
+            const int st = in.unit_starts[u], ln = in.unit_lengths[u];
+            if (st < 0 || ln < 0 || st + ln > in.num_combos)
+                return fail(FLR_E_INVALID_ARGUMENT, "unit_starts/unit_lengths outside the links");
+            if (in.channels[u] < 0 || in.channels[u] > 2)
+                return fail(FLR_E_INVALID_ARGUMENT, "channels must be 0, 1 or 2");
+            s.unit_start[u] = st;
+            s.unit_len[u] = ln;
+            s.base_slot[u] = slot_of(orbits, in.tdi_base_link[u]);
+            if (s.base_slot[u] < 0)
+                return fail(FLR_E_INVALID_ARGUMENT, "TDI base link is not an orbit link");
+            s.channel[u] = in.channels[u];
+            s.sign[u] = in.tdi_signs[u];
+            s.sign_code[u] = (s.sign[u] == 1.0) ? 1 : (s.sign[u] == -1.0) ? -1 : 0;
+            int len = 0;
+            for (int c = st; c < st + ln; ++c) {
+                if (s.combo_slot[c] < 0) continue;
+                if (len == flr::kFusedMaxDepth)
+                    return fail(FLR_E_INVALID_ARGUMENT,
+                                "TDI delay lists may hold at most " +
+                                    std::to_string(flr::kFusedMaxDepth) + " links");
+                s.delay_slot[u][len++] = s.combo_slot[c];
+            }
+            s.delay_len[u] = len;
+            int keep = 0;
+            if (u > 0) {
+                const int lim = std::min(len, s.delay_len[u - 1]);
+                while (keep < lim && s.delay_slot[u][keep] == s.delay_slot[u - 1][keep]) ++keep;
+            }
+            s.prefix_keep[u] = keep;
+            max_len = std::max(max_len, len);
+        }
+    }
+
+    // largest light travel time of the orbit table
+    std::vector<double> ltt((size_t)orbits->N * 6);
+    cudaError_t err = cudaMemcpy(ltt.data(), orbits->ltt, ltt.size() * sizeof(double),
+                                 cudaMemcpyDeviceToHost);
+    if (err != cudaSuccess) return cuda_fail(err, "reading the orbit table");
+    double lmax = 0.0;
+    for (double v : ltt) lmax = std::max(lmax, std::fabs(v));
+
+    flr_batch_plan *p = new flr_batch_plan();
+    p->device = orbits->device;
+    p->mixed = (precision == FLR_PRECISION_MIXED);
+    p->num_sets = num_sets;
+    p->set_max_len = max_len;
+    const int y_halo = (int)std::ceil(max_len * lmax * sampling_frequency) + h + 3;
+    const int spread = (int)std::ceil(2.0 * lmax * sampling_frequency) + 2;
+    p->base.tile = tile;
+    p->base.y_halo = y_halo;
+    p->base.y_max = tile + 2 * y_halo;
+    p->base.win_max = tile + 2 * y_halo + 2 * h + spread + 2 * 4 + 16;
+    p->smem = flr::fused_smem_bytes(p->mixed, p->base.win_max, p->base.y_max);
+
+    // device copies of A, E, the double-float A table and the sets
+    const size_t a_bytes = sizeof(double) * (size_t)num_A;
+    const size_t e_bytes = sizeof(double) * (size_t)std::max(h - 1, 1);
+    const size_t atab_off = (a_bytes + e_bytes + 255) & ~size_t(255);
+    const size_t set_off = (atab_off + sizeof(float4) * (size_t)num_A + 255) & ~size_t(255);
+    std::vector<double> a_host(num_A);
+    err = cudaMemcpy(a_host.data(), A_in, a_bytes, cudaMemcpyDefault);
+    if (err != cudaSuccess) {
+        release(p);
+        return cuda_fail(err, "reading the A table");
+    }
+    std::vector<float4> a_tab(num_A);
+    for (int i = 0; i < num_A; ++i) {
+        const double a = a_host[i];
+        const double da = (i + 1 < num_A) ? a_host[i + 1] - a_host[i] : 0.0;
+        const float ah = (float)a, dah = (float)da;
+        a_tab[i] = make_float4(ah, (float)(a - (double)ah), dah, (float)(da - (double)dah));
+    }
+    err = cudaMalloc(&p->d_tables, set_off + sizeof(flr::FusedTdiSet) * num_sets);
+    if (err == cudaSuccess)
+        err = cudaMemcpy(static_cast<char *>(p->d_tables) + atab_off, a_tab.data(),
+                         sizeof(float4) * (size_t)num_A, cudaMemcpyHostToDevice);
+    if (err == cudaSuccess)
+        err = cudaMemcpy(p->d_tables, A_in, a_bytes, cudaMemcpyDefault);
+    if (err == cudaSuccess && h > 1)
+        err = cudaMemcpy(static_cast<char *>(p->d_tables) + a_bytes, E_in,
+                         sizeof(double) * (h - 1), cudaMemcpyDefault);
+    if (err == cudaSuccess)
+        err = cudaMemcpy(static_cast<char *>(p->d_tables) + set_off, hsets.data(),
+                         sizeof(flr::FusedTdiSet) * num_sets, cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaEventCreateWithFlags(&p->stage_free, cudaEventDisableTiming);
+    int per_sm = 0;
+    if (err == cudaSuccess) err = flr::fused_configure(p->mixed, p->smem, &per_sm);
+    int sms = 0;
+    if (err == cudaSuccess)
+        err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
+    if (err != cudaSuccess) {
+        release(p);
+        return cuda_fail(err, "creating the batch plan");
+    }
+    if (per_sm < 1) {
+        release(p);
+        return fail(FLR_E_UNSUPPORTED, "the fused kernel does not fit on an SM with " +
+                                           std::to_string(p->smem) + " B of shared memory");
+    }
+    p->grid_max = sms * per_sm;
+
+    flr::FusedArgs &b = p->base;
+    b.orb = flr::device_tables(orbits);
+    b.lt.A = static_cast<const double *>(p->d_tables);
+    b.lt.E = reinterpret_cast<const double *>(static_cast<char *>(p->d_tables) + a_bytes);
+    b.lt.deps = deps;
+    b.lt.num_A = num_A;
+    b.lt.h = h;
+    b.sets = reinterpret_cast<const flr::FusedTdiSet *>(static_cast<char *>(p->d_tables) +
+                                                       set_off);
+    b.num_sets = num_sets;
+    b.a_tab = reinterpret_cast<const float4 *>(static_cast<char *>(p->d_tables) + atab_off);
+    b.fs = sampling_frequency;
+    b.dt = 1.0 / sampling_frequency;
+    b.inv_deps = 1.0 / deps;
+    b.inv_orbit_dt = 1.0 / orbits->dt;
+    *out = p;
+    return FLR_OK;
+}
+
+int flr_batch_plan_destroy(flr_batch_plan *plan) {
+    if (!plan) return FLR_OK;
+    if (plan->stage_pending) cudaEventSynchronize(plan->stage_free);
+    release(plan);
+    return FLR_OK;
+}
+
+int flr_batch_plan_info(const flr_batch_plan *plan, int *info, int n_info) {
+    if (!plan || !info) return fail(FLR_E_INVALID_ARGUMENT, "NULL argument");
+    const int vals[] = {plan->base.tile, plan->base.y_halo, plan->base.win_max,
+                        plan->base.y_max, (int)plan->smem, plan->grid_max,
+                        plan->mixed ? FLR_PRECISION_MIXED : FLR_PRECISION_FP64};
+    for (int i = 0; i < n_info && i < (int)(sizeof(vals) / sizeof(int)); ++i) info[i] = vals[i];
+    return FLR_OK;
+}
+
+int flr_batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int num_sources,
+                  int chan, void *stream) {
+    flr::set_last_error("");
+    if (!plan) return fail(FLR_E_INVALID_ARGUMENT, "plan must not be NULL");
+    int rc = current_device_is(plan->device);
+    if (rc) return rc;
+    if (num_sources < 0 || (num_sources > 0 && !sources))
+        return fail(FLR_E_INVALID_ARGUMENT, "invalid source list");
+    if (chan != FLR_CHAN_XYZ && chan != FLR_CHAN_AET && chan != FLR_CHAN_AE)
+        return fail(FLR_E_INVALID_ARGUMENT, "chan must be FLR_CHAN_XYZ, _AET or _AE");
+    const int tile = plan->base.tile;
+    std::vector<flr::FusedSource> srcs(num_sources);
+    size_t num_work = 0;
+    for (int i = 0; i < num_sources; ++i) {
+        const flr_batch_source &s = sources[i];
+        if (!s.h || !s.out || s.n < 2 || s.projections_start < 0 ||
+            s.tdi_start < s.projections_start || 2LL * s.tdi_start >= s.n ||
+            s.n > (1LL << 31) - 1 || s.tdi_set < 0 || s.tdi_set >= plan->num_sets)
+            return fail(FLR_E_INVALID_ARGUMENT,
+                        "source " + std::to_string(i) +
+                            ": need h, out, 0 <= projections_start <= tdi_start < n/2, "
+                            "n < 2^31 and a valid tdi_set");
+        if (reinterpret_cast<uintptr_t>(s.h) % 16 != 0)
+            return fail(FLR_E_INVALID_ARGUMENT, "source " + std::to_string(i) +
+                                                    ": h (complex128) must be 16-byte aligned");
+        flr::FusedSource &d = srcs[i];
+        d.h = static_cast<const double2 *>(s.h);
+        d.out = s.out;
+        d.n = (long)s.n;
+        d.ps = s.projections_start;
+        d.ts = s.tdi_start;
+        d.t0 = s.t0;
+        for (int c = 0; c < 3; ++c) {
+            d.k[c] = s.k[c];
+            d.u[c] = s.u[c];
+            d.v[c] = s.v[c];
+        }
+        d.tdi_set = s.tdi_set;
+        d.pad = 0;
+        num_work += (size_t)((s.n - 2LL * s.tdi_start + tile - 1) / tile);
+    }
+    if (num_work == 0) return FLR_OK;
+    if (num_work > (size_t)0x7fffffff) return fail(FLR_E_INVALID_ARGUMENT, "too many tiles");
+
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t err = cudaSuccess;
+    // the pinned staging buffer of the previous run must have been consumed
+    if (plan->stage_pending) {
+        err = cudaEventSynchronize(plan->stage_free);
+        if (err != cudaSuccess) return cuda_fail(err, "waiting for the previous run's copies");
+        plan->stage_pending = false;
+    }
+    const size_t src_bytes = sizeof(flr::FusedSource) * srcs.size();
+    const size_t work_off = (src_bytes + 255) & ~size_t(255);
+    const size_t stage_bytes = work_off + sizeof(int2) * num_work;
+    if (stage_bytes > plan->cap_stage) {
+        if (plan->h_stage) cudaFreeHost(plan->h_stage);
+        plan->h_stage = nullptr;
+        plan->cap_stage = 0;
+        err = cudaMallocHost(&plan->h_stage, stage_bytes * 2);
+        if (err != cudaSuccess) return cuda_fail(err, "allocating the staging buffer");
+        plan->cap_stage = stage_bytes * 2;
+    }
+    if (srcs.size() > plan->cap_sources) {
+        if (plan->d_sources) cudaFree(plan->d_sources);
+        plan->d_sources = nullptr;
+        plan->cap_sources = 0;
+        err = cudaMalloc(&plan->d_sources, src_bytes * 2);
+        if (err != cudaSuccess) return cuda_fail(err, "allocating source descriptors");
+        plan->cap_sources = srcs.size() * 2;
+    }
+    if (num_work > plan->cap_work) {
+        if (plan->d_work) cudaFree(plan->d_work);
+        plan->d_work = nullptr;
+        plan->cap_work = 0;
+        err = cudaMalloc(&plan->d_work, sizeof(int2) * num_work * 2);
+        if (err != cudaSuccess) return cuda_fail(err, "allocating the work list");
+        plan->cap_work = num_work * 2;
+    }
+    std::memcpy(plan->h_stage, srcs.data(), src_bytes);
+    int2 *work = reinterpret_cast<int2 *>(plan->h_stage + work_off);
+    size_t w = 0;
+    for (int i = 0; i < num_sources; ++i) {
+        const long tiles = (long)((sources[i].n - 2LL * sources[i].tdi_start + tile - 1) / tile);
+        for (long t = 0; t < tiles; ++t) work[w++] = make_int2(i, (int)t);
+    }
+    err = cudaMemcpyAsync(plan->d_sources, plan->h_stage, src_bytes, cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(plan->d_work, work, sizeof(int2) * num_work, cudaMemcpyHostToDevice,
+                              st);
+    if (err == cudaSuccess) err = cudaEventRecord(plan->stage_free, st);
+    if (err != cudaSuccess) return cuda_fail(err, "copying the work list");
+    plan->stage_pending = true;
+
+    flr::FusedArgs a = plan->base;
+    a.sources = plan->d_sources;
+    a.work = plan->d_work;
+    a.num_work = (int)num_work;
+    a.chan = chan;
+    const int grid = (int)std::min<size_t>(num_work, (size_t)plan->grid_max);
+    err = flr::launch_fused(plan->mixed, a, grid, plan->smem, st);
+    if (err != cudaSuccess) return cuda_fail(err, "launching the fused kernel");
+    return FLR_OK;
+}
+
+}  // extern "C"

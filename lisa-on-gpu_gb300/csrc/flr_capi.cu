@@ -11,22 +11,6 @@
 #include "../../include/flr_gb300.h"
 #include "flr_internal.h"
 
-struct flr_orbits {
-    int device;
-    double dt;
-    int N;
-    double armlength;
-    int links[6];
-    int sc_r[6];
-    int sc_e[6];
-    void *block;          // one device allocation holding everything below
-    double *ltt;          // [N][6]
-    double *x;            // [N][9]
-    double *ltt_slope;    // [N-1][6]
-    double *x_slope;      // [N-1][9]
-    unsigned *status;     // status word
-};
-
 namespace {
 
 thread_local std::string g_last_error;
@@ -54,7 +38,9 @@ int check_device(const flr_orbits *o) {
     return FLR_OK;
 }
 
-flr::OrbitTables device_tables(const flr_orbits *o) {
+}  // namespace
+
+flr::OrbitTables flr::device_tables(const flr_orbits *o) {
     flr::OrbitTables t;
     t.dt = o->dt;
     t.N = o->N;
@@ -70,6 +56,8 @@ flr::OrbitTables device_tables(const flr_orbits *o) {
     t.status = o->status;
     return t;
 }
+
+namespace {
 
 int check_lagrange(int order, const double *A, double deps, int num_A, const double *E,
                    flr::LagrangeTables &lt) {
@@ -214,7 +202,7 @@ int flr_get_response(flr_orbits *orbits, double *y_gw, const double *t_data, con
         return fail(FLR_E_INVALID_ARGUMENT, "input_in (complex128) must be 16-byte aligned");
     if (!(sampling_frequency > 0.0))
         return fail(FLR_E_INVALID_ARGUMENT, "sampling_frequency must be positive");
-    a.orb = device_tables(orbits);
+    a.orb = flr::device_tables(orbits);
     a.y_gw = y_gw;
     a.t_data = t_data;
     a.k = k_in;
@@ -253,7 +241,7 @@ int flr_get_tdi_delays(flr_orbits *orbits, double *delayed_links, const double *
         return fail(FLR_E_INVALID_ARGUMENT, "invalid sizes");
     if (!(sampling_frequency > 0.0))
         return fail(FLR_E_INVALID_ARGUMENT, "sampling_frequency must be positive");
-    a.orb = device_tables(orbits);
+    a.orb = flr::device_tables(orbits);
     a.out = delayed_links;
     a.y = input_links;
     a.num_inputs = num_inputs;
@@ -285,7 +273,7 @@ int flr_response_delay_indices(flr_orbits *orbits, int *d_rec, int *d_em, const 
     if (num_delays < 1 || projections_start_ind < 0 || !(sampling_frequency > 0.0))
         return fail(FLR_E_INVALID_ARGUMENT, "invalid sizes");
     flr::ResponseArgs a{};
-    a.orb = device_tables(orbits);
+    a.orb = flr::device_tables(orbits);
     a.t_data = t_data;
     a.k = k_in;
     a.num_delays = num_delays;
@@ -310,7 +298,7 @@ int flr_tdi_delay_indices(flr_orbits *orbits, int *d_tdi, int num_delays, const 
         !(sampling_frequency > 0.0))
         return fail(FLR_E_INVALID_ARGUMENT, "invalid sizes");
     flr::TdiArgs a{};
-    a.orb = device_tables(orbits);
+    a.orb = flr::device_tables(orbits);
     a.num_delays = num_delays;
     a.t_arr = t_arr;
     a.unit_starts = unit_starts;

@@ -124,40 +124,60 @@ __device__ __forceinline__ bool prefactor(const LagrangeTables &lt, double eps, 
     return true;
 }
 
+// Sample sources for the interpolation: read-only global memory through the
+// texture path, or shared memory (staged windows).
+struct GlobalF64 {
+    const double *p;
+    __device__ __forceinline__ double operator[](long i) const { return __ldg(p + i); }
+};
+struct GlobalC128 {
+    const double2 *p;
+    __device__ __forceinline__ double2 operator[](long i) const { return __ldg(p + i); }
+};
+struct SharedF64 {
+    const double *p;
+    __device__ __forceinline__ double operator[](long i) const { return p[i]; }
+};
+struct SharedC128 {
+    const double2 *p;
+    __device__ __forceinline__ double2 operator[](long i) const { return p[i]; }
+};
+
 // Real 2h-point Lagrange interpolation of x around sample d (interp_single,
 // LISAResponse.cu:110-147).  The caller guarantees d-h+1 >= 0 and d+h < n.
-__device__ __forceinline__ double lagrange_real(const double *__restrict__ x, int d, double eps,
-                                                double a, const LagrangeTables &lt) {
+template <class Src>
+__device__ __forceinline__ double lagrange_real(const Src &x, int d, double eps, double a,
+                                                const LagrangeTables &lt) {
     double w_up = 1.0 - eps, w_dn = eps, w_tail = eps * (1.0 - eps);
     double tail = 0.0;
     for (int j = 1; j < lt.h; ++j) {
         double f = (double)j + eps;
         double g = (double)j + (1.0 - eps);
-        double up = __ldg(x + d + 1 + j);
-        double dn = __ldg(x + d - j);
+        double up = x[d + 1 + j];
+        double dn = x[d - j];
         tail += __ldg(lt.E + j - 1) * (up / f + dn / g);
     }
-    return a * (w_up * __ldg(x + d + 1) + w_dn * __ldg(x + d) + w_tail * tail);
+    return a * (w_up * x[d + 1] + w_dn * x[d] + w_tail * tail);
 }
 
 // Complex version over interleaved complex128 samples (interp,
-// LISAResponse.cu:149-207).  x must be 16-byte aligned.
-__device__ __forceinline__ void lagrange_c128(const double2 *__restrict__ x, int d, double eps,
-                                              double a, const LagrangeTables &lt, double &re,
-                                              double &im) {
+// LISAResponse.cu:149-207).
+template <class Src>
+__device__ __forceinline__ void lagrange_c128(const Src &x, int d, double eps, double a,
+                                              const LagrangeTables &lt, double &re, double &im) {
     double w_up = 1.0 - eps, w_dn = eps, w_tail = eps * (1.0 - eps);
     double tail_re = 0.0, tail_im = 0.0;
     for (int j = 1; j < lt.h; ++j) {
         double f = (double)j + eps;
         double g = (double)j + (1.0 - eps);
-        double2 up = __ldg(x + d + 1 + j);
-        double2 dn = __ldg(x + d - j);
+        double2 up = x[d + 1 + j];
+        double2 dn = x[d - j];
         double e = __ldg(lt.E + j - 1);
         tail_re += e * (up.x / f + dn.x / g);
         tail_im += e * (up.y / f + dn.y / g);
     }
-    double2 up0 = __ldg(x + d + 1);
-    double2 dn0 = __ldg(x + d);
+    double2 up0 = x[d + 1];
+    double2 dn0 = x[d];
     re = a * (w_up * up0.x + w_dn * dn0.x + w_tail * tail_re);
     im = a * (w_up * up0.y + w_dn * dn0.y + w_tail * tail_im);
 }

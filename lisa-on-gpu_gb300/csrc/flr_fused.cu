@@ -1,0 +1,677 @@
+// Batched, fused response + TDI (sm_103a): one persistent launch over a
+// flattened (source, tile) work list.
+//
+// A work item is T consecutive output samples [o0, o1) of one source.  The CTA
+//   1. finds the input window its link streams need (geometry at the two ends
+//      of the stream range), and stages it into shared memory with one 1-D
+//      bulk copy (cp.async.bulk, mbarrier completion, bounded wait);
+//   2. computes the six link streams y for [o0 - halo, o1 + halo) into shared
+//      memory (one (link, sample) per thread iteration);
+//   3. computes the TDI channels of [o0, o1) from those streams (one output
+//      sample, all units of all channels, per thread iteration) and writes
+//      X/Y/Z (or A/E/T, A/E) to global memory.
+// The link streams never touch HBM: per output sample the kernel reads 16 B
+// of input and writes 24 B (plus the halos).
+//
+// Two arithmetic flavours share this structure:
+//   exact: every interpolation, geometry and index operation is the plain
+//          path's (flr_device.cuh): outputs are bit-identical to the reference's
+//          CPU arithmetic.  Bound by the FP64 pipe.
+//   mixed: delays, their integer/fractional split, orbit interpolation and TDI
+//          delay sums in FP64 with the same operation order (integer indices
+//          bit-exact); the Lagrange taps, weights and projections in
+//          double-float arithmetic (flr_df.cuh) on the FP32 pipe, with the tile's
+//          input scaled by a power of two near 1/max|h|.  The link response is
+//          formed by summation by parts, sum_k W_k x_k =
+//          P_b x_b - sum_{k<b} P_k (x_{k+1} - x_k) with P the running weight
+//          sums, so the cancellation between the emitter and receiver terms
+//          happens on first differences of the input instead of on the input.
+//
+// Compiled with --fmad=false (required by both flavours).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "flr_df.cuh"
+#include "flr_device.cuh"
+#include "flr_fused.h"
+
+namespace flr {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWindowMargin = 4;          // samples added on each side of the window estimate
+constexpr long kMaxWaitPolls = 1L << 20;  // bound on mbarrier polls for one bulk copy
+constexpr unsigned kStatusStaging = 0x10u;
+
+__device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000ll); }
+
+// ------------------------------------------------------------ bulk copy ----
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// 1-D bulk copy global -> shared; src and dst 16-byte aligned, bytes a
+// multiple of 16.
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes,
+                                              uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the bulk copy of the current phase; true when it completed.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+    for (long it = 0; it < kMaxWaitPolls; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// ------------------------------------------------------- shared layout ----
+
+struct Layout {
+    size_t set, edf, hraw, hdf, dh, y, total;
+};
+
+__host__ __device__ constexpr size_t align128(size_t x) { return (x + 127) & ~size_t(127); }
+
+__host__ __device__ inline Layout layout(bool mixed, int win_max, int y_max) {
+    Layout L{};
+    size_t off = 256;  // mbarrier, scale, window bounds, warp maxima
+    L.set = off;
+    off = align128(off + sizeof(FusedTdiSet));
+    L.edf = off;
+    off = align128(off + sizeof(df::f2) * kFusedMaxH);
+    L.hraw = off;
+    off = align128(off + sizeof(double2) * (size_t)win_max);
+    if (mixed) {
+        L.hdf = off;
+        off = align128(off + sizeof(float4) * (size_t)win_max);
+        L.dh = off;
+        off = align128(off + sizeof(float4) * (size_t)win_max);
+        L.y = off;
+        off = align128(off + sizeof(float2) * 6 * (size_t)y_max);
+    } else {
+        L.hdf = L.dh = 0;
+        L.y = off;
+        off = align128(off + sizeof(double) * 6 * (size_t)y_max);
+    }
+    L.total = off;
+    return L;
+}
+
+// ------------------------------------------------- mixed-path geometry ----
+
+// Segment index of the orbit grid found by multiplication with 1/dt; equal to
+// orbit_segment()'s (int)(t / dt) because the two quotients differ by a few
+// ulp and the exact division is used whenever t/dt is that close to an
+// integer.
+__device__ __forceinline__ int orbit_segment_fast(const OrbitTables &o, double inv_dt, double t) {
+    double q = t * inv_dt;
+    double r = rint(q);
+    int w = (fabs(q - r) <= 1e-9 * fmax(1.0, fabs(q))) ? (int)(t / o.dt) : (int)q;
+    if (w < 0 || w > o.N - 1) return -1;
+    return (w == o.N - 1) ? o.N - 2 : w;
+}
+
+__device__ __forceinline__ void position_seg(const OrbitTables &o, int w, double t, int sc,
+                                             double out[3]) {
+    int s = (sc >= 1 && sc <= 3) ? sc - 1 : -1;
+    if (w < 0 || s < 0) {
+        out[0] = out[1] = out[2] = 0.0;
+        return;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) out[c] = orbit_lerp(o.x, o.x_slope, w, 9, 3 * s + c, t, o.dt);
+}
+
+struct MixedDelays {
+    int d_rec, d_em;
+    double e_rec, e_em;
+    double x_rec[3], x_em[3];
+};
+
+// Receiver/emitter delays exactly as link_geometry() computes them (same
+// operations, same order, so the integer indices are bit-identical), plus
+// the spacecraft positions for the projection factors.
+__device__ __forceinline__ MixedDelays link_delays_mixed(const OrbitTables &o, double inv_dt,
+                                                         int slot, double t, double t_first,
+                                                         double fs, const double k[3]) {
+    MixedDelays g;
+    int w = orbit_segment_fast(o, inv_dt, t);
+    double L = (w < 0) ? 0.0 : orbit_lerp(o.ltt, o.ltt_slope, w, 6, slot, t, o.dt);
+    double t_em = t - L;
+    position_seg(o, w, t, o.sc_r[slot], g.x_rec);
+    position_seg(o, orbit_segment_fast(o, inv_dt, t_em), t_em, o.sc_e[slot], g.x_em);
+    double kx_rec = dot3(k, g.x_rec);
+    double kx_em = dot3(k, g.x_em);
+    split_delay(t - kx_rec * kCInv, t_first, fs, g.d_rec, g.e_rec);
+    split_delay(t_em - kx_em * kCInv, t_first, fs, g.d_em, g.e_em);
+    return g;
+}
+
+// 1/sqrt(x) in df: hardware approximation and one Newton step,
+// r = r0 + r0 (1 - x r0^2) / 2; relative error ~1e-14.
+__device__ __forceinline__ df::f2 df_rsqrt(df::f2 x) {
+    float r0;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(x.hi));
+    const df::f2 xr2 = df::mul_raw(x, df::two_prod(r0, r0));
+    const float t = (1.0f - xr2.hi) - xr2.lo;
+    return df::fast_two_sum(r0, r0 * 0.5f * t);
+}
+
+__device__ __forceinline__ df::f2 df_dot3(const df::f2 a[3], const df::f2 b[3]) {
+    return df::add(df::add(df::mul(a[0], b[0]), df::mul(a[1], b[1])), df::mul(a[2], b[2]));
+}
+
+struct DfProjection {
+    df::f2 xi_p, xi_c, pre;  // polarisation projections and 1 / (1 - k.n)
+};
+
+// Projection factors of one link (LISAResponse.cu:581-606, 664) in df from the
+// FP64 spacecraft positions: n = (x_rec - x_em) / |x_rec - x_em|,
+// xi+ = ((u.n)^2 - (v.n)^2) / 2, xix = (u.n)(v.n), 1 / (1 - k.n).
+__device__ __forceinline__ DfProjection df_projection(const double x_rec[3], const double x_em[3],
+                                                      const df::f2 k[3], const df::f2 u[3],
+                                                      const df::f2 v[3]) {
+    df::f2 n[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) n[c] = df::from_double(x_rec[c] - x_em[c]);
+    const df::f2 r = df_rsqrt(df_dot3(n, n));
+#pragma unroll
+    for (int c = 0; c < 3; ++c) n[c] = df::mul(n[c], r);
+    const df::f2 un = df_dot3(u, n), vn = df_dot3(v, n), kn = df_dot3(k, n);
+    DfProjection p;
+    const df::f2 d = df::sub(df::mul(un, un), df::mul(vn, vn));
+    p.xi_p = {0.5f * d.hi, 0.5f * d.lo};
+    p.xi_c = df::mul(un, vn);
+    p.pre = df::renorm(df::rcp(df::sub({1.0f, 0.0f}, kn)));
+    return p;
+}
+
+// A(eps) from the df table: q = eps / deps, A = A[ind] + (q - ind) (A[ind+1] - A[ind]),
+// the reference's lerp (LISAResponse.cu:114-117) rearranged; differs from it
+// by rounding only.
+__device__ __forceinline__ df::f2 prefactor_df(const float4 *tab, int num_A, df::f2 inv_deps,
+                                               df::f2 e) {
+    const df::f2 q = df::mul_raw(e, inv_deps);
+    const float fl = floorf(q.hi);
+    int ind = (int)fl;
+    if (q.hi == fl && q.lo < 0.f) ind -= 1;
+    ind = min(max(ind, 0), num_A - 2);
+    const df::f2 frac = df::fast_two_sum(q.hi - (float)ind, q.lo);
+    const float4 t = __ldg(tab + ind);
+    return df::add({t.x, t.y}, df::mul_raw(frac, {t.z, t.w}));
+}
+
+// --------------------------------------------- double-float interpolation ----
+
+// Tap weights of the reference's kernel (interp, LISAResponse.cu:149-207):
+// W_{d+1} = A(1-e), W_d = A e, W_{d+1+j} = A e(1-e) E_j/(j+e),
+// W_{d-j} = A e(1-e) E_j/(j+1-e), j = 1..h-1.
+struct DfWeights {
+    df::f2 A, e, ome, c;  // A, eps, 1 - eps, A eps (1 - eps)
+};
+
+__device__ __forceinline__ DfWeights df_weights(df::f2 A, df::f2 e) {
+    DfWeights w;
+    w.A = A;
+    w.e = e;
+    w.ome = df::sub({1.0f, 0.0f}, e);
+    w.c = df::mul(df::mul(A, e), w.ome);
+    return w;
+}
+
+__device__ __forceinline__ df::f2 df_tail_up(const DfWeights &w, df::f2 Ej, int j) {
+    return df::mul_raw(df::mul(w.c, Ej), df::rcp(df::add_big_float((float)j, w.e)));
+}
+
+__device__ __forceinline__ df::f2 df_tail_dn(const DfWeights &w, df::f2 Ej, int j) {
+    return df::mul_raw(df::mul(w.c, Ej), df::rcp(df::add_big_float((float)j, w.ome)));
+}
+
+// Shared-memory df views of the staged input: value and first difference.
+struct DfShared {
+    const float4 *x;   // (re_hi, re_lo, im_hi, im_lo)
+    const float4 *dx;  // x[k+1] - x[k]
+    __device__ __forceinline__ float4 val(long k) const { return x[k]; }
+    __device__ __forceinline__ float4 diff(long k) const { return dx[k]; }
+};
+
+// The same views computed on the fly from global memory (used when a tap
+// window falls outside the staged window).
+struct DfGlobal {
+    const double2 *h;
+    double scale;
+    __device__ __forceinline__ float4 val(long k) const {
+        double2 v = __ldg(h + k);
+        df::f2 r = df::from_double(v.x * scale), i = df::from_double(v.y * scale);
+        return make_float4(r.hi, r.lo, i.hi, i.lo);
+    }
+    __device__ __forceinline__ float4 diff(long k) const {
+        double2 a = __ldg(h + k), b = __ldg(h + k + 1);
+        df::f2 r = df::from_double((b.x - a.x) * scale), i = df::from_double((b.y - a.y) * scale);
+        return make_float4(r.hi, r.lo, i.hi, i.lo);
+    }
+};
+
+// Complex interpolation around sample d of the source, by summation by parts.
+template <class Src>
+__device__ __forceinline__ void df_interp_c128_sbp(const Src &src, long d, df::f2 A, df::f2 eps,
+                                                   const df::f2 *edf, int h, df::f2 &re,
+                                                   df::f2 &im) {
+    const DfWeights w = df_weights(A, eps);
+    df::f2 P = {0.f, 0.f};
+    df::Acc sre, sim;
+    df::acc_init(sre);
+    df::acc_init(sim);
+    auto step = [&](df::f2 W, long k) {
+        P = df::add(P, W);
+        float4 dx = src.diff(k);
+        df::acc_fma(sre, P, {dx.x, dx.y});
+        df::acc_fma(sim, P, {dx.z, dx.w});
+    };
+    for (int j = h - 1; j >= 1; --j) step(df_tail_dn(w, edf[j - 1], j), d - j);
+    step(df::mul_raw(w.A, w.e), d);
+    df::f2 W_last;
+    long last;
+    if (h == 1) {
+        W_last = df::mul_raw(w.A, w.ome);
+        last = d + 1;
+    } else {
+        step(df::mul_raw(w.A, w.ome), d + 1);
+        for (int j = 1; j < h - 1; ++j) step(df_tail_up(w, edf[j - 1], j), d + 1 + j);
+        W_last = df_tail_up(w, edf[h - 2], h - 1);
+        last = d + h;
+    }
+    P = df::add(P, W_last);
+    float4 xb = src.val(last);
+    re = df::sub(df::mul(P, {xb.x, xb.y}), df::acc_value(sre));
+    im = df::sub(df::mul(P, {xb.z, xb.w}), df::acc_value(sim));
+}
+
+// Real interpolation around sample d of a staged df link row, compensated dot
+// product (Dot2).
+__device__ __forceinline__ df::f2 df_interp_real(const float2 *y, int d, df::f2 A, df::f2 eps,
+                                                 const df::f2 *edf, int h) {
+    const DfWeights w = df_weights(A, eps);
+    df::Acc acc;
+    df::acc_init(acc);
+    float2 v = y[d + 1];
+    df::acc_fma(acc, df::mul_raw(w.A, w.ome), {v.x, v.y});
+    v = y[d];
+    df::acc_fma(acc, df::mul_raw(w.A, w.e), {v.x, v.y});
+    for (int j = 1; j < h; ++j) {
+        const df::f2 cE = df::mul(w.c, edf[j - 1]);
+        float2 up = y[d + 1 + j], dn = y[d - j];
+        df::acc_fma(acc, df::mul_raw(cE, df::rcp(df::add_big_float((float)j, w.e))),
+                    {up.x, up.y});
+        df::acc_fma(acc, df::mul_raw(cE, df::rcp(df::add_big_float((float)j, w.ome))),
+                    {dn.x, dn.y});
+    }
+    return df::acc_value(acc);
+}
+
+// -------------------------------------------------------------- the kernel ----
+
+template <bool kMixed>
+__global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const Layout lay = layout(kMixed, a.win_max, a.y_max);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    double *scale_sm = reinterpret_cast<double *>(smem + 16);
+    int *win_sm = reinterpret_cast<int *>(smem + 32);  // [0] = min d, [1] = max d
+    double *warp_max = reinterpret_cast<double *>(smem + 64);
+    FusedTdiSet *set = reinterpret_cast<FusedTdiSet *>(smem + lay.set);
+    df::f2 *edf = reinterpret_cast<df::f2 *>(smem + lay.edf);
+    double2 *hraw = reinterpret_cast<double2 *>(smem + lay.hraw);
+    float4 *hdf = reinterpret_cast<float4 *>(smem + lay.hdf);
+    float4 *dh = reinterpret_cast<float4 *>(smem + lay.dh);
+    double *y64 = reinterpret_cast<double *>(smem + lay.y);
+    float2 *y32 = reinterpret_cast<float2 *>(smem + lay.y);
+
+    const int tid = threadIdx.x;
+    const int h = a.lt.h;
+    const df::f2 inv_deps_df = df::from_double(a.inv_deps);
+    if (tid == 0) mbar_init(bar, 1);
+    for (int j = tid; j < h - 1; j += kThreads) edf[j] = df::from_double(__ldg(a.lt.E + j));
+    __syncthreads();
+
+    uint32_t phase = 0;
+    int loaded_set = -1;
+    for (int wi = blockIdx.x; wi < a.num_work; wi += gridDim.x) {
+        const int2 item = a.work[wi];
+        const FusedSource &src = a.sources[item.x];
+        const long n = src.n;
+        const int ps = src.ps, ts = src.ts;
+        const double t0 = src.t0;
+        const double k[3] = {src.k[0], src.k[1], src.k[2]};
+        const double u[3] = {src.u[0], src.u[1], src.u[2]};
+        const double v[3] = {src.v[0], src.v[1], src.v[2]};
+        df::f2 kdf[3], udf[3], vdf[3];
+        if (kMixed) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                kdf[c] = df::from_double(k[c]);
+                udf[c] = df::from_double(u[c]);
+                vdf[c] = df::from_double(v[c]);
+            }
+        }
+
+        if (src.tdi_set != loaded_set) {
+            const int *from = reinterpret_cast<const int *>(a.sets + src.tdi_set);
+            int *to = reinterpret_cast<int *>(set);
+            for (int i = tid; i < (int)(sizeof(FusedTdiSet) / sizeof(int)); i += kThreads)
+                to[i] = from[i];
+            loaded_set = src.tdi_set;
+        }
+
+        const long o0 = ts + (long)item.y * a.tile;
+        const long o1 = min(o0 + (long)a.tile, n - ts);
+        const long ya = max(o0 - a.y_halo, 0L);
+        const long yb = min(o1 + a.y_halo, n);
+        const long yfirst = max(ya, (long)ps), ylast = min(yb, n - ps);  // y computed here
+        const int Y = (int)(yb - ya);
+
+        // 1. input window: delays at both ends of the computed stream range
+        if (tid == 0) {
+            win_sm[0] = 0x7fffffff;
+            win_sm[1] = -0x7fffffff;
+        }
+        __syncthreads();
+        if (tid < 12 && yfirst < ylast) {
+            const int slot = tid % 6;
+            const long j = (tid < 6) ? yfirst : ylast - 1;
+            const double t = t0 + (double)j * a.dt;
+            int dr, de;
+            if (kMixed) {
+                MixedDelays g = link_delays_mixed(a.orb, a.inv_orbit_dt, slot, t, t0, a.fs, k);
+                dr = g.d_rec;
+                de = g.d_em;
+            } else {
+                LinkGeometry g = link_geometry(a.orb, slot, t, t0, a.fs, k, u, v);
+                dr = g.d_rec;
+                de = g.d_em;
+            }
+            atomicMin(&win_sm[0], min(dr, de));
+            atomicMax(&win_sm[1], max(dr, de));
+        }
+        __syncthreads();
+        long wlo = 0;
+        int W = 0;
+        if (yfirst < ylast) {
+            wlo = max((long)win_sm[0] - (h - 1) - kWindowMargin, 0L);
+            const long whi = min((long)win_sm[1] + h + 1 + kWindowMargin, n);
+            W = (int)max(0L, min(whi - wlo, (long)a.win_max));
+        }
+
+        // 2. stage the window with one bulk copy
+        if (W > 0) {
+            if (tid == 0) {
+                fence_proxy_async();
+                mbar_expect_tx(bar, (uint32_t)W * 16u);
+                bulk_copy_g2s(hraw, src.h + wlo, (uint32_t)W * 16u, bar);
+            }
+            const bool done = mbar_wait_bounded(bar, phase);
+            if (__syncthreads_or(!done)) {
+                if (tid == 0) raise_status(a.orb.status, kStatusStaging);
+                mbar_wait_bounded(bar, phase);  // let a late copy land before exiting
+                return;
+            }
+            phase ^= 1u;
+        }
+
+        // 3. mixed: scale to ~1 by a power of two, split into df, first differences
+        double scale = 1.0;
+        if (kMixed) {
+            double m = 0.0;
+            for (int i = tid; i < W; i += kThreads) {
+                double2 q = hraw[i];
+                m = fmax(m, fmax(fabs(q.x), fabs(q.y)));
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+            if ((tid & 31) == 0) warp_max[tid >> 5] = m;
+            __syncthreads();
+            if (tid == 0) {
+                double mm = 0.0;
+                for (int i = 0; i < kThreads / 32; ++i) mm = fmax(mm, warp_max[i]);
+                int ex = 0;
+                double s = 1.0;
+                if (mm > 0.0 && mm < 1e300) {
+                    frexp(mm, &ex);
+                    s = ldexp(1.0, -ex);
+                }
+                *scale_sm = s;
+            }
+            __syncthreads();
+            scale = *scale_sm;
+            for (int i = tid; i < W; i += kThreads) {
+                const double2 q = hraw[i];
+                df::f2 r = df::from_double(q.x * scale), im = df::from_double(q.y * scale);
+                hdf[i] = make_float4(r.hi, r.lo, im.hi, im.lo);
+                if (i + 1 < W) {
+                    const double2 q1 = hraw[i + 1];
+                    df::f2 dr = df::from_double((q1.x - q.x) * scale);
+                    df::f2 di = df::from_double((q1.y - q.y) * scale);
+                    dh[i] = make_float4(dr.hi, dr.lo, di.hi, di.lo);
+                }
+            }
+        }
+        __syncthreads();
+
+        // 4. link streams y[slot][j - ya] for j in [ya, yb)
+        for (int it = tid; it < 6 * Y; it += kThreads) {
+            const int slot = it / Y;
+            const int jj = it - slot * Y;
+            const long j = ya + jj;
+            if (j < yfirst || j >= ylast) {  // the reference's y_gw is zero there
+                if (kMixed)
+                    y32[slot * a.y_max + jj] = make_float2(0.f, 0.f);
+                else
+                    y64[slot * a.y_max + jj] = 0.0;
+                continue;
+            }
+            const double t = t0 + (double)j * a.dt;
+            if (kMixed) {
+                const MixedDelays g = link_delays_mixed(a.orb, a.inv_orbit_dt, slot, t, t0, a.fs, k);
+                const long lo = (long)min(g.d_rec, g.d_em) - (h - 1);
+                const long hi = (long)max(g.d_rec, g.d_em) + h;
+                const df::f2 e_r = df::from_double(g.e_rec), e_e = df::from_double(g.e_em);
+                const df::f2 A_r = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_r);
+                const df::f2 A_e = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_e);
+                df::f2 re_r, im_r, re_e, im_e;
+                if (lo >= wlo && hi + 1 < wlo + W) {
+                    const DfShared s{hdf, dh};
+                    df_interp_c128_sbp(s, g.d_rec - wlo, A_r, e_r, edf, h, re_r, im_r);
+                    df_interp_c128_sbp(s, g.d_em - wlo, A_e, e_e, edf, h, re_e, im_e);
+                } else if (lo >= 0 && hi + 1 < n) {
+                    const DfGlobal s{src.h, scale};
+                    df_interp_c128_sbp(s, g.d_rec, A_r, e_r, edf, h, re_r, im_r);
+                    df_interp_c128_sbp(s, g.d_em, A_e, e_e, edf, h, re_e, im_e);
+                } else {
+                    raise_status(a.orb.status, kStatusTap);
+                    y32[slot * a.y_max + jj] = make_float2(__int_as_float(0x7fc00000), 0.f);
+                    continue;
+                }
+                const DfProjection pr = df_projection(g.x_rec, g.x_em, kdf, udf, vdf);
+                const df::f2 dre = df::sub(re_e, re_r), dim = df::sub(im_e, im_r);
+                df::f2 yv = df::add(df::mul(dre, pr.xi_p), df::mul(dim, pr.xi_c));
+                yv = df::mul(yv, pr.pre);
+                y32[slot * a.y_max + jj] = make_float2(yv.hi, yv.lo);
+            } else {
+                const LinkGeometry g = link_geometry(a.orb, slot, t, t0, a.fs, k, u, v);
+                const long lo = (long)min(g.d_rec, g.d_em) - (h - 1);
+                const long hi = (long)max(g.d_rec, g.d_em) + h;
+                double A_r, A_e, out;
+                bool ok = prefactor(a.lt, g.e_rec, A_r);
+                ok = prefactor(a.lt, g.e_em, A_e) && ok;
+                if (!ok) {
+                    raise_status(a.orb.status, kStatusAIndex);
+                    out = qnan();
+                } else if ((lo >= wlo && hi < wlo + W) || (lo >= 0 && hi < n)) {
+                    double hp_r, hc_r, hp_e, hc_e;
+                    if (lo >= wlo && hi < wlo + W) {
+                        const SharedC128 s{hraw};
+                        lagrange_c128(s, (int)(g.d_rec - wlo), g.e_rec, A_r, a.lt, hp_r, hc_r);
+                        lagrange_c128(s, (int)(g.d_em - wlo), g.e_em, A_e, a.lt, hp_e, hc_e);
+                    } else {
+                        const GlobalC128 s{src.h};
+                        lagrange_c128(s, g.d_rec, g.e_rec, A_r, a.lt, hp_r, hc_r);
+                        lagrange_c128(s, g.d_em, g.e_em, A_e, a.lt, hp_e, hc_e);
+                    }
+                    double pre = 1. / (1. - g.k_dot_n);
+                    double big = (hp_e - hp_r) * g.xi_p + (hc_e - hc_r) * g.xi_c;
+                    out = pre * big;
+                } else {
+                    raise_status(a.orb.status, kStatusTap);
+                    out = qnan();
+                }
+                y64[slot * a.y_max + jj] = out;
+            }
+        }
+        __syncthreads();
+
+        // 5. TDI for the output samples [o0, o1)
+        const double inv_scale = 1.0 / scale;
+        for (long i = o0 + tid; i < o1; i += kThreads) {
+            const double t = t0 + (double)i * a.dt;
+            double L[kLinks];
+            if (kMixed) {
+                const int w = orbit_segment_fast(a.orb, a.inv_orbit_dt, t);
+#pragma unroll
+                for (int s = 0; s < kLinks; ++s)
+                    L[s] = (w < 0) ? 0.0 : orbit_lerp(a.orb.ltt, a.orb.ltt_slope, w, 6, s, t,
+                                                      a.orb.dt);
+            } else {
+#pragma unroll
+                for (int s = 0; s < kLinks; ++s) L[s] = light_travel_time(a.orb, t, s);
+            }
+            double acc64[3] = {0.0, 0.0, 0.0};
+            df::f2 accdf[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+            double stack[kFusedMaxDepth + 1];  // partial delays t - L_1 - ... - L_s
+            stack[0] = t;
+            for (int unit = 0; unit < set->num_units; ++unit) {
+                const int ch = set->channel[unit];
+                const int len = set->delay_len[unit];
+                for (int s = set->prefix_keep[unit]; s < len; ++s)
+                    stack[s + 1] = stack[s] - L[set->delay_slot[unit][s]];
+                const double delay = stack[len];
+                int d;
+                double eps;
+                split_delay(delay, t0, a.fs, d, eps);
+                const int b = set->base_slot[unit];
+                const long lo = (long)d - (h - 1), hi = (long)d + h;
+                if (lo < ya || hi >= yb) {
+                    raise_status(a.orb.status, kStatusTap);
+                    acc64[ch] = qnan();
+                    accdf[ch] = {__int_as_float(0x7fc00000), 0.f};
+                    continue;
+                }
+                if (kMixed) {
+                    const df::f2 e = df::from_double(eps);
+                    const df::f2 A = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e);
+                    df::f2 val = df_interp_real(y32 + b * a.y_max, (int)(d - ya), A, e, edf, h);
+                    const int sc = set->sign_code[unit];
+                    if (sc == 1)
+                        accdf[ch] = df::add(accdf[ch], val);
+                    else if (sc == -1)
+                        accdf[ch] = df::sub(accdf[ch], val);
+                    else
+                        accdf[ch] = df::add(accdf[ch], df::mul(val, df::from_double(set->sign[unit])));
+                } else {
+                    double pre;
+                    if (!prefactor(a.lt, eps, pre)) {
+                        raise_status(a.orb.status, kStatusAIndex);
+                        acc64[ch] = qnan();
+                        continue;
+                    }
+                    const SharedF64 row{y64 + b * a.y_max};
+                    double val = lagrange_real(row, (int)(d - ya), eps, pre, a.lt);
+                    val *= set->sign[unit];
+                    acc64[ch] += val;
+                }
+            }
+            double X, Yc, Z;
+            if (kMixed) {
+                X = df::to_double(accdf[0]) * inv_scale;
+                Yc = df::to_double(accdf[1]) * inv_scale;
+                Z = df::to_double(accdf[2]) * inv_scale;
+            } else {
+                X = acc64[0];
+                Yc = acc64[1];
+                Z = acc64[2];
+            }
+            double *out = src.out;
+            if (a.chan == kChanXYZ) {
+                out[i] = X;
+                out[n + i] = Yc;
+                out[2 * n + i] = Z;
+            } else {
+                // lisaanalysistools AET: (Z-X)/sqrt2, (X-2Y+Z)/sqrt6, (X+Y+Z)/sqrt3
+                out[i] = (Z - X) / 1.4142135623730951;
+                out[n + i] = (X - 2.0 * Yc + Z) / 2.449489742783178;
+                if (a.chan == kChanAET) out[2 * n + i] = (X + Yc + Z) / 1.7320508075688772;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+size_t fused_smem_bytes(bool mixed, int win_max, int y_max) {
+    return layout(mixed, win_max, y_max).total;
+}
+
+cudaError_t fused_configure(bool mixed, size_t smem_bytes, int *blocks_per_sm) {
+    const void *fn = mixed ? reinterpret_cast<const void *>(fused_kernel<true>)
+                           : reinterpret_cast<const void *>(fused_kernel<false>);
+    cudaError_t err =
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    if (err != cudaSuccess) return err;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, kThreads, smem_bytes);
+}
+
+cudaError_t launch_fused(bool mixed, const FusedArgs &a, int grid, size_t smem_bytes,
+                         cudaStream_t stream) {
+    if (a.num_work <= 0) return cudaSuccess;
+    if (mixed)
+        fused_kernel<true><<<grid, kThreads, smem_bytes, stream>>>(a);
+    else
+        fused_kernel<false><<<grid, kThreads, smem_bytes, stream>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace flr

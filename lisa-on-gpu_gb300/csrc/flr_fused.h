@@ -1,0 +1,75 @@
+// Internal interface of the batched, fused response + TDI kernel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "flr_device.cuh"
+
+namespace flr {
+
+constexpr int kFusedMaxUnits = 64;
+constexpr int kFusedMaxCombos = 320;
+constexpr int kFusedMaxDepth = 16;  // links per TDI delay list
+constexpr int kFusedMaxH = 40;   // h = (order + 1) / 2 supported by the fused kernel
+
+// One source of a batch (device copy of flr_batch_source plus derived values).
+struct FusedSource {
+    const double2 *h;   // [n] complex128 input
+    double *out;        // [3][n] output channels, rows of length n
+    long n;
+    int ps;             // projections_start_ind: y is zero outside [ps, n - ps)
+    int ts;             // tdi_start_ind: outputs are computed for [ts, n - ts)
+    double t0;          // time of sample 0
+    double k[3], u[3], v[3];
+    int tdi_set;        // index into the TDI table sets
+    int pad;
+};
+
+// TDI unit tables with link numbers already mapped to link slots.
+struct FusedTdiSet {
+    int num_units;
+    int num_combos;
+    int unit_start[kFusedMaxUnits];
+    int unit_len[kFusedMaxUnits];
+    int base_slot[kFusedMaxUnits];
+    int channel[kFusedMaxUnits];
+    double sign[kFusedMaxUnits];
+    int sign_code[kFusedMaxUnits];    // +1, -1, or 0 (general sign: multiply)
+    // Delay lists in compact form: unit u subtracts L of link_slot[u][0..len-1]
+    // (the "no delay" markers removed), and shares its first prefix_keep[u]
+    // partial sums with unit u-1, whose partial sums are bitwise the ones u
+    // would compute itself (same subtractions in the same order).
+    int delay_len[kFusedMaxUnits];
+    int prefix_keep[kFusedMaxUnits];
+    int delay_slot[kFusedMaxUnits][kFusedMaxDepth];
+    int combo_slot[kFusedMaxCombos];  // -1: no delay
+};
+
+enum FusedChan { kChanXYZ = 0, kChanAET = 1, kChanAE = 2 };
+
+struct FusedArgs {
+    OrbitTables orb;
+    LagrangeTables lt;
+    const FusedSource *sources;
+    const int2 *work;          // (source, tile) items
+    int num_work;
+    const FusedTdiSet *sets;
+    int num_sets;
+    const float4 *a_tab;       // per A-table knot: (A hi, A lo, dA hi, dA lo), dA = A[k+1]-A[k]
+    int tile;                  // output samples per work item
+    int y_halo;                // link-stream samples computed on each side of a tile
+    int win_max;               // capacity of the staged input window [samples]
+    int y_max;                 // capacity of one staged link row [samples]
+    double fs;                 // sampling frequency
+    double dt;                 // 1 / fs as the host computes it (t_i = t0 + i * dt)
+    double inv_deps;           // 1 / deps
+    double inv_orbit_dt;       // 1 / orbit dt
+    int chan;                  // FusedChan
+};
+
+size_t fused_smem_bytes(bool mixed, int win_max, int y_max);
+cudaError_t fused_configure(bool mixed, size_t smem_bytes, int *blocks_per_sm);
+cudaError_t launch_fused(bool mixed, const FusedArgs &a, int grid, size_t smem_bytes,
+                         cudaStream_t stream);
+
+}  // namespace flr

@@ -7,7 +7,27 @@
 
 #include "flr_device.cuh"
 
+// Orbit handle of the C ABI (opaque to callers).
+struct flr_orbits {
+    int device;
+    double dt;
+    int N;
+    double armlength;
+    int links[6];
+    int sc_r[6];
+    int sc_e[6];
+    void *block;          // one device allocation holding everything below
+    double *ltt;          // [N][6]
+    double *x;            // [N][9]
+    double *ltt_slope;    // [N-1][6]
+    double *x_slope;      // [N-1][9]
+    unsigned *status;     // status word
+};
+
 namespace flr {
+
+// Kernel-side view of an orbit handle.
+OrbitTables device_tables(const flr_orbits *o);
 
 struct ResponseArgs {
     OrbitTables orb;

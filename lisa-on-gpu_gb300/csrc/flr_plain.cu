@@ -64,8 +64,9 @@ response_plain_kernel(ResponseArgs a) {
         return;
     }
     double hp_rec, hc_rec, hp_em, hc_em;
-    lagrange_c128(a.input, g.d_rec, g.e_rec, A_rec, a.lt, hp_rec, hc_rec);
-    lagrange_c128(a.input, g.d_em, g.e_em, A_em, a.lt, hp_em, hc_em);
+    const GlobalC128 src{a.input};
+    lagrange_c128(src, g.d_rec, g.e_rec, A_rec, a.lt, hp_rec, hc_rec);
+    lagrange_c128(src, g.d_em, g.e_em, A_em, a.lt, hp_em, hc_em);
 
     double pre = 1. / (1. - g.k_dot_n);
     double big = (hp_em - hp_rec) * g.xi_p + (hc_em - hc_rec) * g.xi_c;
@@ -130,7 +131,8 @@ tdi_plain_kernel(TdiArgs a) {
             acc = quiet_nan();
             continue;
         }
-        double val = lagrange_real(a.y + (size_t)base * a.num_inputs, d, eps, pre, a.lt);
+        const GlobalF64 row{a.y + (size_t)base * a.num_inputs};
+        double val = lagrange_real(row, d, eps, pre, a.lt);
         val *= __ldg(a.signs + unit);
         acc += val;
     }

@@ -8,6 +8,7 @@ C ABI in ``include/flr_gb300.h``) through ctypes.  There is no CPU backend.
 
 from ._build import build, needs_build
 from ._lib import FLRError, describe_status, library_path
+from .batch import BatchedResponseTDI
 from .binding import LISAResponseWrap, LISAResponseWrapGPU, OrbitsWrap, OrbitsWrapGPU_responselisa
 from .orbits import EqualArmlengthOrbits, KeplerianOrbits, Orbits
 from .response import (ResponseWrapper, lagrange_tables, pyResponseTDI, sky_basis,
@@ -18,7 +19,7 @@ from .waveforms import GBWave, gb_waveform, time_grid
 __version__ = "0.1.0"
 
 __all__ = [
-    "AET", "EqualArmlengthOrbits", "FLRError", "GBWave", "KeplerianOrbits",
+    "AET", "BatchedResponseTDI", "EqualArmlengthOrbits", "FLRError", "GBWave", "KeplerianOrbits",
     "LISAResponseWrap", "LISAResponseWrapGPU", "Orbits", "OrbitsWrap",
     "OrbitsWrapGPU_responselisa", "ResponseWrapper", "build", "describe_status",
     "gb_waveform", "get_overlap", "lagrange_tables", "library_path", "needs_build",

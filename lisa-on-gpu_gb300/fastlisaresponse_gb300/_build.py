@@ -31,6 +31,8 @@ SOURCES = {
     "flr_capi.cu": [],
     "flr_probe.cu": [],
     "flr_noalloc.cu": ["--fmad=false"],
+    "flr_fused.cu": ["--fmad=false"],
+    "flr_batch.cu": [],
 }
 
 _lock = threading.Lock()
