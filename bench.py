@@ -241,6 +241,97 @@ def load_traffic(kernel: str, workload: str):
     return None if entry is None else entry.get("bytes_per_launch")
 
 
+def _events():
+    import torch
+
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def _timed(fn, steps, warmup, device, kernel_events=None):
+    """Run fn warmup + steps times; CUDA-event time of the steps [s]."""
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize(device)
+    e0, e1 = _events()
+    if kernel_events is not None:
+        kernel_events["on"] = True
+    e0.record()
+    for _ in range(steps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize(device)
+    if kernel_events is not None:
+        kernel_events["on"] = False
+    return e0.elapsed_time(e1) * 1e-3
+
+
+def _rel_l2_rows(got, want):
+    import torch
+
+    worst = 0.0
+    for r in range(want.shape[0]):
+        den = torch.linalg.vector_norm(want[r]).item()
+        num = torch.linalg.vector_norm(got[r] - want[r]).item()
+        worst = max(worst, num / den if den > 0 else num)
+    return worst
+
+
+def _config3_sources(count, seed, dt, device):
+    """Sources drawn like the batching configuration: lengths log-uniform in
+    2^15..2^22 samples, f log-U 1e-4..1e-2 Hz, fdot log-U 1e-18..1e-13,
+    A log-U 1e-23..1e-21, isotropic angles; waveforms generated on the device."""
+    import torch
+
+    from fastlisaresponse_gb300 import waveforms as wf
+
+    rng = np.random.default_rng(seed)
+    lengths = np.exp(rng.uniform(np.log(2**15), np.log(2**22), count)).astype(np.int64)
+    p = wf.draw_gb_parameters(rng, count)
+    hs = []
+    for i, n in enumerate(lengths):
+        t = torch.arange(int(n), dtype=torch.float64, device=device) * dt
+        hs.append(wf.gb_waveform(p["A"][i], p["f"][i], p["fdot"][i], p["iota"][i],
+                                 p["phi0"][i], p["psi"][i], t))
+    return lengths, hs, p["lam"], p["beta"]
+
+
+def run_batch_section(args, device, peaks):
+    """Config-3-shaped batch: mixed vs FP64 fused kernels, same sources."""
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+
+    dt = 10.0
+    lengths, hs, lam, beta = _config3_sources(args.batch_sources, seed=3, dt=dt, device=device)
+    orb = flr.EqualArmlengthOrbits(t_max=(math.floor(lengths.max() * dt / 1e4) + 3) * 1e4)
+    n_out = int(sum(int(n) - 2 * int(T_BUFFER / dt) for n in lengths))
+    res = {"sources": int(args.batch_sources), "samples": int(lengths.sum()),
+           "output_samples": n_out,
+           "workload": "config-3-shaped batch: lengths log-uniform 2^15..2^22 at dt = 10 s, "
+                       "f log-U 1e-4..1e-2 Hz, equal-arm orbits, 2nd-gen TDI XYZ, order 25"}
+    outs = {}
+    for prec, steps in (("mixed", args.steps), ("fp64", 1)):
+        bat = flr.BatchedResponseTDI(1 / dt, order=25, tdi="2nd generation", orbits=orb,
+                                     precision=prec)
+        holder = {}
+
+        def step():
+            holder["o"] = bat(hs, lam, beta)
+
+        secs = _timed(step, steps, 1, device)
+        assert bat.status() == 0, flr.describe_status(bat.status())
+        outs[prec] = holder["o"]
+        res[prec] = {"value": n_out * steps / secs, "ms_per_step": 1e3 * secs / steps,
+                     "steps": steps, "plan": bat.plan_info}
+        del bat
+    res["speedup_mixed_over_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
+    res["max_rel_l2_mixed_vs_fp64"] = max(_rel_l2_rows(a, b) for a, b in
+                                          zip(outs["mixed"], outs["fp64"]))
+    return res
+
+
 def run_ours(args, rank, world, device):
     import torch
 
@@ -250,139 +341,165 @@ def run_ours(args, rank, world, device):
     w = WORKLOADS[args.workload]
     n, dt = w["n"], w["dt"]
     orb, h, lam, beta = make_source(w, n, seed=1 + rank)
-    resp = flr.pyResponseTDI(1.0 / dt, n, order=w["order"], tdi=w["tdi"], orbits=orb,
-                             force_backend=device)
     n_out = output_samples(n, dt)
     h_dev = torch.as_tensor(h, device=device)
     lib = _lib.lib()
     peaks = measure_fp64_peak(lib, device)
 
-    # per-kernel CUDA events around the two launches (recorded on the stream the
-    # binding launches on: torch's current stream)
-    ev = {"response": [], "tdi": []}
-    rec = {"on": False}
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # --- headline: mixed-precision fused path (BatchedResponseTDI, one source)
+    bat = flr.BatchedResponseTDI(1.0 / dt, order=w["order"], tdi=w["tdi"], orbits=orb,
+                                 precision="mixed", force_backend=device)
+    ev = {"on": False, "fused": []}
+    run_fn = lib.flr_batch_run
+
+    def timed_run(*a):
+        if not ev["on"]:
+            return run_fn(*a)
+        e0, e1 = _events()
+        e0.record()
+        rc = run_fn(*a)
+        e1.record()
+        ev["fused"].append((e0, e1))
+        return rc
+
+    lib.flr_batch_run = timed_run
+    held = {}
+
+    def mixed_step():
+        held["mixed"] = bat([h_dev], lam, beta)[0]
+
+    for _ in range(args.warmup):
+        mixed_step()
+    torch.cuda.synchronize(device)
+    clocks = ClockSampler(gpu_uuid(device))
+    clocks.start()
+    time.sleep(0.4)
+    barrier()
+    elapsed = _timed(mixed_step, args.steps, 0, device, kernel_events=ev)
+    barrier()
+    clock_info = clocks.stop()
+    lib.flr_batch_run = run_fn
+    assert bat.status() == 0, flr.describe_status(bat.status())
+
+    # --- the plain FP64 drop-in path on the same source
+    resp = flr.pyResponseTDI(1.0 / dt, n, order=w["order"], tdi=w["tdi"], orbits=orb,
+                             force_backend=device)
+    pev = {"on": False, "response": [], "tdi": []}
 
     def wrap(name, fn):
         def inner(*a, **k):
-            if not rec["on"]:
+            if not pev["on"]:
                 return fn(*a, **k)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
+            e0, e1 = _events()
             e0.record()
             fn(*a, **k)
             e1.record()
-            ev[name].append((e0, e1))
+            pev[name].append((e0, e1))
         return inner
 
     resp.cpp_response.get_response_wrap = wrap("response", resp.cpp_response.get_response_wrap)
     resp.cpp_response.get_tdi_delays_wrap = wrap("tdi", resp.cpp_response.get_tdi_delays_wrap)
 
-    def device_step():
+    def plain_step():
         resp.get_projections(h_dev, lam, beta, t0=0.0, t_buffer=T_BUFFER)
         resp.get_tdi_delays()
 
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
+    plain_steps = max(1, min(args.steps, 5))
+    plain_elapsed = _timed(plain_step, plain_steps, 1, device, kernel_events=pev)
+    assert resp.status() == 0
+    max_rel = _rel_l2_rows(held["mixed"], resp.XYZ)
 
-    for _ in range(args.warmup):
-        device_step()
-    torch.cuda.synchronize(device)
-
-    clocks = ClockSampler(gpu_uuid(device))
-    clocks.start()
-    time.sleep(0.4)
-    barrier()
-    torch.cuda.synchronize(device)
-    rec["on"] = True
-    start = torch.cuda.Event(enable_timing=True)
-    stop = torch.cuda.Event(enable_timing=True)
-    start.record()
-    for _ in range(args.steps):
-        device_step()
-    stop.record()
-    torch.cuda.synchronize(device)
-    rec["on"] = False
-    barrier()
-    clock_info = clocks.stop()
-    elapsed = start.elapsed_time(stop) * 1e-3
-    assert resp.status() == 0, flr.describe_status(resp.status())
-
-    # end-to-end: pinned host input -> device -> response + TDI -> pinned host X/Y/Z
+    # --- end to end through BatchedResponseTDI: pinned host in, pinned host out
     h_pin = torch.from_numpy(h).pin_memory()
     out_pin = torch.empty((3, n), dtype=torch.float64).pin_memory()
+    out_dev = torch.zeros((3, n), dtype=torch.float64, device=device)
 
     def e2e_step():
-        resp.get_projections(h_pin, lam, beta, t0=0.0, t_buffer=T_BUFFER)
-        resp.get_tdi_delays()
-        out_pin.copy_(resp.XYZ, non_blocking=True)
+        bat([h_pin], lam, beta, out=[out_dev])
+        out_pin.copy_(out_dev, non_blocking=True)
 
-    for _ in range(args.warmup):
-        e2e_step()
-    torch.cuda.synchronize(device)
     barrier()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
-        e2e_step()
-    e1.record()
-    torch.cuda.synchronize(device)
+    e2e_elapsed = _timed(e2e_step, args.steps, args.warmup, device)
     barrier()
-    e2e_elapsed = e0.elapsed_time(e1) * 1e-3
 
-    # max over ranks
     times = torch.tensor([elapsed, e2e_elapsed], dtype=torch.float64, device=device)
     if world > 1:
         torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
     elapsed, e2e_elapsed = float(times[0]), float(times[1])
 
-    kern_ms = {k: 1e3 * statistics.mean(a.elapsed_time(b) * 1e-3 for a, b in v)
-               for k, v in ev.items()}
+    # --- rooflines
     tables = resp.tdi_tables_host
-    n_delay_links = int(np.count_nonzero(tables["tdi_link_combinations"] != -11))
-    counts = perfmodel.counts_per_sample(w["order"], tables["num_units"], n_delay_links)
-    computed = {"response": n - 2 * resp.projections_start_ind,
-                "tdi": n - 2 * resp.tdi_start_ind}
-    dominant = max(kern_ms, key=kern_ms.get)
-    secs = kern_ms[dominant] * 1e-3
-    peak = peaks["fp64_fma"]
-    div_cost = peaks["fp64_fma"] / peaks["fp64_div"]
-    c = counts[dominant]
-    slots = perfmodel.fp64_slots(c, div_cost) * computed[dominant]
-    plain_ops = (c["ops"] + c["divs"]) * computed[dominant]
-    launch_bytes = perfmodel.BYTES_PER_SAMPLE[dominant] * computed[dominant]
+    lists = []
+    for u in range(tables["num_units"]):
+        st, ln = tables["unit_starts"][u], tables["unit_lengths"][u]
+        lists.append([x for x in tables["tdi_link_combinations"][st:st + ln] if x != -11])
+    n_delay_links = sum(len(x) for x in lists)
     measured = {}
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(peaks_path):
         with open(peaks_path) as fh:
             measured = json.load(fh)
     hbm_peak = measured.get("hbm_gbs")
-    kernel_name = {"response": "response_plain_kernel", "tdi": "tdi_plain_kernel"}[dominant]
+    peak = peaks["fp64_fma"]
+    div_cost = peaks["fp64_fma"] / peaks["fp64_div"]
+
+    fused_ms = 1e3 * statistics.mean(a.elapsed_time(b) * 1e-3 for a, b in ev["fused"])
+    idx_ops = perfmodel.mixed_index_ops(tables["num_units"],
+                                        perfmodel.prefix_shared_subtractions(lists))
+    fused_secs = fused_ms * 1e-3
+    fused_bytes = 40 * n_out  # complex input in, three channels out
     roofline = {
         "bound": "fp64",
-        "kernel": kernel_name,
-        "achieved": slots / secs / 1e9,
+        "kernel": "fused_kernel<mixed> (flr_fused.cu)",
+        "achieved": idx_ops["total"] * n_out / fused_secs / 1e9,
         "peak": peak / 1e9,
-        "unit": "G FP64-slots/s",
-        "frac": slots / secs / peak,
-        "definition": "algorithmic FP64 work of the reference arithmetic per output sample "
-                      "(perfmodel.counts_per_sample: ops + divs, here "
-                      f"{c['ops']} + {c['divs']} for {dominant}), each division or square "
-                      f"root weighted by its measured cost of {div_cost:.2f} FMA slots "
-                      "(probe: FMA rate / divide rate), over the launch's CUDA-event time",
-        "frac_division_as_one_op": plain_ops / secs / peak,
+        "unit": "G FP64-ops/s",
+        "frac": idx_ops["total"] * n_out / fused_secs / peak,
+        "definition": "FP64 operations the bit-exact delay/index path needs per output "
+                      f"sample (perfmodel.mixed_index_ops: {idx_ops['total']}), over the "
+                      "launch's CUDA-event time; the double-float taps run on the FP32 pipe "
+                      "and are not counted",
         "peak_source": "measured in this run: FP64 FMA probe kernel (flr_probe_pipe_rate), "
                        "best of 3; MEASURED_PEAKS.json has no FP64 figure",
-        "launch_ms": kern_ms[dominant],
-        "algorithmic_bytes": launch_bytes,
-        "traffic": load_traffic(kernel_name, args.workload),
-        "hbm": {"achieved_gbs": launch_bytes / secs / 1e9,
-                "peak_gbs": hbm_peak,
-                "frac": (launch_bytes / secs / 1e9 / hbm_peak) if hbm_peak else None,
+        "launch_ms": fused_ms,
+        "algorithmic_bytes": fused_bytes,
+        "traffic": load_traffic("fused_kernel_mixed", args.workload),
+        "hbm": {"achieved_gbs": fused_bytes / fused_secs / 1e9, "peak_gbs": hbm_peak,
+                "frac": (fused_bytes / fused_secs / 1e9 / hbm_peak) if hbm_peak else None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if hbm_peak else None},
-        "kernels_ms": kern_ms,
         "pipe_peaks_g_per_s": {k: v / 1e9 for k, v in peaks.items() if k != "sms"},
+    }
+    kern = {k: 1e3 * statistics.mean(a.elapsed_time(b) * 1e-3 for a, b in pev[k])
+            for k in ("response", "tdi")}
+    counts = perfmodel.counts_per_sample(w["order"], tables["num_units"], n_delay_links)
+    computed = {"response": n - 2 * resp.projections_start_ind,
+                "tdi": n - 2 * resp.tdi_start_ind}
+    dominant = max(kern, key=kern.get)
+    c = counts[dominant]
+    slots = perfmodel.fp64_slots(c, div_cost) * computed[dominant]
+    psecs = kern[dominant] * 1e-3
+    plain = {
+        "value": n_out * plain_steps / plain_elapsed,
+        "ms_per_step": 1e3 * plain_elapsed / plain_steps,
+        "steps": plain_steps,
+        "path": "pyResponseTDI.get_projections + get_tdi_delays (two plain FP64 kernels, "
+                "bit-identical to the reference's CPU arithmetic)",
+        "kernels_ms": kern,
+        "roofline": {
+            "bound": "fp64", "kernel": f"{dominant}_plain_kernel",
+            "achieved": slots / psecs / 1e9, "peak": peak / 1e9, "unit": "G FP64-slots/s",
+            "frac": slots / psecs / peak,
+            "frac_division_as_one_op": (c["ops"] + c["divs"]) * computed[dominant] / psecs / peak,
+            "definition": "reference-arithmetic FP64 work (perfmodel.counts_per_sample: "
+                          f"{c['ops']} ops + {c['divs']} divisions per sample for {dominant}), "
+                          f"divisions weighted by their measured cost ({div_cost:.2f} FMA "
+                          "slots)",
+            "traffic": load_traffic(f"{dominant}_plain_kernel", args.workload),
+        },
     }
     result = {
         "metric": METRIC,
@@ -395,19 +512,28 @@ def run_ours(args, rank, world, device):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
+        "dtype": "f64 delays/indices + double-float (2xf32) taps; outputs f64",
         "data": "synthetic (seeded galactic-binary waveform, analytic orbits)",
         "config": {"workload": w["desc"], "name": args.workload, "samples_per_step": n_out,
-                   "input_samples": n, "path": "plain FP64 (bit-identical to the reference "
-                   "CPU arithmetic)", "l2": "inputs larger than L2: h 16 B + y_gw 48 B + XYZ "
-                   f"24 B per sample = {88 * n / 1e6:.0f} MB per step"},
+                   "input_samples": n,
+                   "path": "mixed-precision fused kernel (BatchedResponseTDI, one source); "
+                           "integer delay indices bit-exact",
+                   "l2": "inputs larger than L2: h 16 B + XYZ 24 B per sample = "
+                         f"{40 * n / 1e6:.0f} MB per step"},
+        "accuracy": {"max_rel_l2_vs_plain_fp64": max_rel, "bound": 1e-6,
+                     "per": "TDI channel, this run's outputs"},
+        "plain_fp64": plain,
+        "speedup_vs_plain_fp64": (n_out * args.steps / elapsed) / plain["value"],
         "e2e": {"value": n_out * args.steps * world / e2e_elapsed, "unit": UNIT,
                 "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 24 * n,
-                "api": "pyResponseTDI.get_projections + get_tdi_delays, pinned host buffers"},
-        "gpu_launches": 2 * args.steps,
+                "api": "BatchedResponseTDI.__call__ with the input in pinned host memory, "
+                       "X/Y/Z copied to pinned host memory"},
+        "gpu_launches": args.steps,
         "roofline": roofline,
         "clocks": clock_info,
     }
+    if args.batch_sources > 0 and world == 1:
+        result["batched"] = run_batch_section(args, device, peaks)
     return result
 
 
@@ -456,6 +582,8 @@ def main():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-sources", type=int, default=256,
+                    help="sources in the config-3-shaped batch section (0 = skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
 

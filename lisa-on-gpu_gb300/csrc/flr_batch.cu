@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -106,7 +107,24 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
     if (tile == 0) tile = 512;
     if (tile < 32 || tile > 8192) return fail(FLR_E_INVALID_ARGUMENT, "tile must be in [32, 8192]");
 
-    // TDI sets: map link numbers to slots, check sizes
+    // largest light travel time of the orbit table; equal-arm tables (all six
+    // links equal at every knot) give equal delays to lists of equal length
+    std::vector<double> ltt((size_t)orbits->N * 6);
+    cudaError_t err = cudaMemcpy(ltt.data(), orbits->ltt, ltt.size() * sizeof(double),
+                                 cudaMemcpyDeviceToHost);
+    if (err != cudaSuccess) return cuda_fail(err, "reading the orbit table");
+    double lmax = 0.0;
+    bool equal_arms = true;
+    for (size_t i = 0; i < ltt.size(); ++i) {
+        lmax = std::max(lmax, std::fabs(ltt[i]));
+        if (ltt[i] != ltt[(i / 6) * 6]) equal_arms = false;
+    }
+    const bool mixed = (precision == FLR_PRECISION_MIXED);
+
+    // TDI sets: map link numbers to slots, check sizes.  The FP64 flavour keeps
+    // the reference's unit order (its per-channel sums are order-sensitive);
+    // the mixed flavour on equal-arm orbits orders units by delay-list length
+    // so that units with equal delays are adjacent and share the index split.
     std::vector<flr::FusedTdiSet> hsets(num_sets);
     int max_len = 0;
     for (int si = 0; si < num_sets; ++si) {
@@ -129,19 +147,32 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
                 return fail(FLR_E_INVALID_ARGUMENT,
                             "TDI link " + std::to_string(link) + " is not an orbit link");
         }
+        std::vector<int> order(in.num_units);
+        for (int u = 0; u < in.num_units; ++u) order[u] = u;
+        if (mixed && equal_arms) {
+            auto list_len = [&](int u) {
+                int len = 0;
+                for (int c = in.unit_starts[u]; c < in.unit_starts[u] + in.unit_lengths[u]; ++c)
+                    len += (c >= 0 && c < in.num_combos && in.tdi_link_combinations[c] != -11);
+                return len;
+            };
+            std::stable_sort(order.begin(), order.end(),
+                             [&](int a, int b) { return list_len(a) < list_len(b); });
+        }
         for (int u = 0; u < in.num_units; ++u) {
-            const int st = in.unit_starts[u], ln = in.unit_lengths[u];
+            const int src_u = order[u];
+            const int st = in.unit_starts[src_u], ln = in.unit_lengths[src_u];
             if (st < 0 || ln < 0 || st + ln > in.num_combos)
                 return fail(FLR_E_INVALID_ARGUMENT, "unit_starts/unit_lengths outside the links");
-            if (in.channels[u] < 0 || in.channels[u] > 2)
+            if (in.channels[src_u] < 0 || in.channels[src_u] > 2)
                 return fail(FLR_E_INVALID_ARGUMENT, "channels must be 0, 1 or 2");
             s.unit_start[u] = st;
             s.unit_len[u] = ln;
-            s.base_slot[u] = slot_of(orbits, in.tdi_base_link[u]);
+            s.base_slot[u] = slot_of(orbits, in.tdi_base_link[src_u]);
             if (s.base_slot[u] < 0)
                 return fail(FLR_E_INVALID_ARGUMENT, "TDI base link is not an orbit link");
-            s.channel[u] = in.channels[u];
-            s.sign[u] = in.tdi_signs[u];
+            s.channel[u] = in.channels[src_u];
+            s.sign[u] = in.tdi_signs[src_u];
             s.sign_code[u] = (s.sign[u] == 1.0) ? 1 : (s.sign[u] == -1.0) ? -1 : 0;
             int len = 0;
             for (int c = st; c < st + ln; ++c) {
@@ -156,24 +187,20 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
             int keep = 0;
             if (u > 0) {
                 const int lim = std::min(len, s.delay_len[u - 1]);
-                while (keep < lim && s.delay_slot[u][keep] == s.delay_slot[u - 1][keep]) ++keep;
+                if (mixed && equal_arms)
+                    keep = lim;  // every L(t) is the same value: partial sums depend on length only
+                else
+                    while (keep < lim && s.delay_slot[u][keep] == s.delay_slot[u - 1][keep]) ++keep;
             }
             s.prefix_keep[u] = keep;
             max_len = std::max(max_len, len);
         }
     }
 
-    // largest light travel time of the orbit table
-    std::vector<double> ltt((size_t)orbits->N * 6);
-    cudaError_t err = cudaMemcpy(ltt.data(), orbits->ltt, ltt.size() * sizeof(double),
-                                 cudaMemcpyDeviceToHost);
-    if (err != cudaSuccess) return cuda_fail(err, "reading the orbit table");
-    double lmax = 0.0;
-    for (double v : ltt) lmax = std::max(lmax, std::fabs(v));
 
     flr_batch_plan *p = new flr_batch_plan();
     p->device = orbits->device;
-    p->mixed = (precision == FLR_PRECISION_MIXED);
+    p->mixed = mixed;
     p->num_sets = num_sets;
     p->set_max_len = max_len;
     const int y_halo = (int)std::ceil(max_len * lmax * sampling_frequency) + h + 3;

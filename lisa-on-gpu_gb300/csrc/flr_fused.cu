@@ -156,6 +156,18 @@ __device__ __forceinline__ void position_seg(const OrbitTables &o, int w, double
     for (int c = 0; c < 3; ++c) out[c] = orbit_lerp(o.x, o.x_slope, w, 9, 3 * s + c, t, o.dt);
 }
 
+// The reference's index split (LISAResponse.cu:339-341, 616-622),
+// d = (int)ceil(y) - 1 and eps = (1 + d) - y with y = (t - t0) * fs, with the
+// ceiling taken by a round-up conversion: (double)(d + 1) equals 1.0 + d, so
+// d and eps are bit-identical to split_delay().
+__device__ __forceinline__ void split_delay_fast(double delayed_t, double t_first, double fs,
+                                                 int &d, double &eps) {
+    const double y = (delayed_t - t_first) * fs;
+    const int c = __double2int_ru(y);
+    d = c - 1;
+    eps = (double)c - y;
+}
+
 struct MixedDelays {
     int d_rec, d_em;
     double e_rec, e_em;
@@ -176,8 +188,8 @@ __device__ __forceinline__ MixedDelays link_delays_mixed(const OrbitTables &o, d
     position_seg(o, orbit_segment_fast(o, inv_dt, t_em), t_em, o.sc_e[slot], g.x_em);
     double kx_rec = dot3(k, g.x_rec);
     double kx_em = dot3(k, g.x_em);
-    split_delay(t - kx_rec * kCInv, t_first, fs, g.d_rec, g.e_rec);
-    split_delay(t_em - kx_em * kCInv, t_first, fs, g.d_em, g.e_em);
+    split_delay_fast(t - kx_rec * kCInv, t_first, fs, g.d_rec, g.e_rec);
+    split_delay_fast(t_em - kx_em * kCInv, t_first, fs, g.d_em, g.e_em);
     return g;
 }
 
@@ -582,15 +594,28 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
             df::f2 accdf[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
             double stack[kFusedMaxDepth + 1];  // partial delays t - L_1 - ... - L_s
             stack[0] = t;
+            long long prev_bits = 0x7ff8dead00000000ll;  // a NaN no delay can equal
+            int d = 0;
+            double eps = 0.0;
+            df::f2 e_df = {0.f, 0.f}, A_df = {0.f, 0.f};
             for (int unit = 0; unit < set->num_units; ++unit) {
                 const int ch = set->channel[unit];
                 const int len = set->delay_len[unit];
                 for (int s = set->prefix_keep[unit]; s < len; ++s)
                     stack[s + 1] = stack[s] - L[set->delay_slot[unit][s]];
                 const double delay = stack[len];
-                int d;
-                double eps;
-                split_delay(delay, t0, a.fs, d, eps);
+                if (kMixed) {
+                    // consecutive units with bit-identical delays share the split
+                    const long long bits = __double_as_longlong(delay);
+                    if (bits != prev_bits) {
+                        split_delay_fast(delay, t0, a.fs, d, eps);
+                        e_df = df::from_double(eps);
+                        A_df = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_df);
+                        prev_bits = bits;
+                    }
+                } else {
+                    split_delay(delay, t0, a.fs, d, eps);
+                }
                 const int b = set->base_slot[unit];
                 const long lo = (long)d - (h - 1), hi = (long)d + h;
                 if (lo < ya || hi >= yb) {
@@ -600,9 +625,8 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
                     continue;
                 }
                 if (kMixed) {
-                    const df::f2 e = df::from_double(eps);
-                    const df::f2 A = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e);
-                    df::f2 val = df_interp_real(y32 + b * a.y_max, (int)(d - ya), A, e, edf, h);
+                    df::f2 val = df_interp_real(y32 + b * a.y_max, (int)(d - ya), A_df, e_df, edf,
+                                                h);
                     const int sc = set->sign_code[unit];
                     if (sc == 1)
                         accdf[ch] = df::add(accdf[ch], val);

@@ -72,3 +72,34 @@ BYTES_PER_SAMPLE = {
     "tdi": 48 + 24,        # six links in, three channels out
 }
 BYTES_PER_SAMPLE["total"] = BYTES_PER_SAMPLE["response"] + BYTES_PER_SAMPLE["tdi"]
+
+
+def mixed_index_ops(num_units: int, delay_subtractions: int) -> dict:
+    """FP64 operations of the mixed path's exact index path per output sample:
+    the work that must stay in FP64 for the integer delays to be bit-exact
+    (orbit lerps of L and positions, k.x, delays, index splits), with each
+    orbit-segment lookup counted as one operation.  `delay_subtractions` is the
+    number of TDI partial sums evaluated per sample (prefix sharing included).
+    Taps, weights and projections run on the FP32 pipe and are not counted."""
+    per_link = (1 + 4      # segment(t), L(t)
+                + 6        # x_rec: 3 coordinates
+                + 1 + 1 + 8  # t_em, segment(t_em), x_em
+                + 2 * 6    # k.x_rec, k.x_em
+                + 2 * 2    # delays
+                + 2 * 6)   # index splits
+    response = 6 * per_link
+    tdi = 1 + 6 * 2 + delay_subtractions + num_units * 6
+    return {"response": response, "tdi": tdi, "total": response + tdi}
+
+
+def prefix_shared_subtractions(delay_lists) -> int:
+    """Partial sums evaluated when each unit reuses the common prefix of the
+    previous unit's delay list (delay_lists: sequence of link sequences)."""
+    total, prev = 0, []
+    for cur in delay_lists:
+        keep = 0
+        while keep < min(len(cur), len(prev)) and cur[keep] == prev[keep]:
+            keep += 1
+        total += len(cur) - keep
+        prev = cur
+    return total
