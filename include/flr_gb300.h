@@ -236,6 +236,19 @@ int flr_batch_plan_info(const flr_batch_plan *plan, int *info, int n_info);
 int flr_batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int num_sources,
                   int chan, void *stream);
 
+/* Galactic-binary parameters: h+ = A(1+cos^2 iota) cos Phi, hx = -2A cos iota
+ * sin Phi, Phi = phi0 + 2 pi (f t + fdot t^2 / 2), rotated by the polarisation
+ * angle psi (hp cos2psi - hx sin2psi, hp sin2psi + hx cos2psi). */
+typedef struct {
+    double A, f, fdot, iota, phi0, psi;
+} flr_gb_params;
+
+/* As flr_batch_run, but first generates each source's waveform on the device
+ * into sources[i].h (a device buffer of n complex128 the caller provides) at
+ * t_i = t0 + i / fs.  One waveform launch and one fused launch per call. */
+int flr_batch_run_gb(flr_batch_plan *plan, const flr_batch_source *sources,
+                     const flr_gb_params *params, int num_sources, int chan, void *stream);
+
 /*
  * Link projections without any device allocation.  No counterpart in the
  * reference: for callers that cannot call cudaMalloc -- code running inside a

@@ -30,10 +30,9 @@ struct flr_batch_plan {
     int num_sets;
     int set_max_len;           // longest TDI delay list (links subtracted)
     void *d_tables;            // A, E and the TDI sets (device)
-    flr::FusedSource *d_sources;
-    size_t cap_sources;
-    int2 *d_work;
-    size_t cap_work;
+    unsigned char *d_stage;    // per-run descriptors, work items, waveform parameters
+    size_t cap_device;
+    int sms;
     unsigned char *h_stage;    // pinned staging for descriptors and work items
     size_t cap_stage;
     cudaEvent_t stage_free;    // recorded after the staging copies of the last run
@@ -71,8 +70,7 @@ int slot_of(const flr_orbits *o, int link) {
 void release(flr_batch_plan *p) {
     if (!p) return;
     if (p->d_tables) cudaFree(p->d_tables);
-    if (p->d_sources) cudaFree(p->d_sources);
-    if (p->d_work) cudaFree(p->d_work);
+    if (p->d_stage) cudaFree(p->d_stage);
     if (p->h_stage) cudaFreeHost(p->h_stage);
     if (p->stage_free) cudaEventDestroy(p->stage_free);
     delete p;
@@ -257,6 +255,7 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
                                            std::to_string(p->smem) + " B of shared memory");
     }
     p->grid_max = sms * per_sm;
+    p->sms = sms;
 
     flr::FusedArgs &b = p->base;
     b.orb = flr::device_tables(orbits);
@@ -293,8 +292,8 @@ int flr_batch_plan_info(const flr_batch_plan *plan, int *info, int n_info) {
     return FLR_OK;
 }
 
-int flr_batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int num_sources,
-                  int chan, void *stream) {
+static int batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int num_sources,
+                     const flr_gb_params *gb, int chan, void *stream) {
     flr::set_last_error("");
     if (!plan) return fail(FLR_E_INVALID_ARGUMENT, "plan must not be NULL");
     int rc = current_device_is(plan->device);
@@ -306,6 +305,8 @@ int flr_batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int num
     const int tile = plan->base.tile;
     std::vector<flr::FusedSource> srcs(num_sources);
     size_t num_work = 0;
+    long num_chunks = 0;
+    std::vector<long> chunk_start(num_sources);
     for (int i = 0; i < num_sources; ++i) {
         const flr_batch_source &s = sources[i];
         if (!s.h || !s.out || s.n < 2 || s.projections_start < 0 ||
@@ -333,6 +334,8 @@ int flr_batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int num
         d.tdi_set = s.tdi_set;
         d.pad = 0;
         num_work += (size_t)((s.n - 2LL * s.tdi_start + tile - 1) / tile);
+        chunk_start[i] = num_chunks;
+        num_chunks += flr::gb_waveform_chunks((long)s.n);
     }
     if (num_work == 0) return FLR_OK;
     if (num_work > (size_t)0x7fffffff) return fail(FLR_E_INVALID_ARGUMENT, "too many tiles");
@@ -345,9 +348,14 @@ int flr_batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int num
         if (err != cudaSuccess) return cuda_fail(err, "waiting for the previous run's copies");
         plan->stage_pending = false;
     }
+    // staging layout: sources | work items | gb params | chunk starts
+    auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
     const size_t src_bytes = sizeof(flr::FusedSource) * srcs.size();
-    const size_t work_off = (src_bytes + 255) & ~size_t(255);
-    const size_t stage_bytes = work_off + sizeof(int2) * num_work;
+    const size_t work_off = up(src_bytes);
+    const size_t gb_off = up(work_off + sizeof(int2) * num_work);
+    const size_t gb_bytes = gb ? sizeof(flr::GbParams) * srcs.size() : 0;
+    const size_t cs_off = up(gb_off + gb_bytes);
+    const size_t stage_bytes = cs_off + (gb ? sizeof(long) * srcs.size() : 0);
     if (stage_bytes > plan->cap_stage) {
         if (plan->h_stage) cudaFreeHost(plan->h_stage);
         plan->h_stage = nullptr;
@@ -356,46 +364,62 @@ int flr_batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int num
         if (err != cudaSuccess) return cuda_fail(err, "allocating the staging buffer");
         plan->cap_stage = stage_bytes * 2;
     }
-    if (srcs.size() > plan->cap_sources) {
-        if (plan->d_sources) cudaFree(plan->d_sources);
-        plan->d_sources = nullptr;
-        plan->cap_sources = 0;
-        err = cudaMalloc(&plan->d_sources, src_bytes * 2);
-        if (err != cudaSuccess) return cuda_fail(err, "allocating source descriptors");
-        plan->cap_sources = srcs.size() * 2;
-    }
-    if (num_work > plan->cap_work) {
-        if (plan->d_work) cudaFree(plan->d_work);
-        plan->d_work = nullptr;
-        plan->cap_work = 0;
-        err = cudaMalloc(&plan->d_work, sizeof(int2) * num_work * 2);
+    if (stage_bytes > plan->cap_device) {
+        if (plan->d_stage) cudaFree(plan->d_stage);
+        plan->d_stage = nullptr;
+        plan->cap_device = 0;
+        err = cudaMalloc(&plan->d_stage, stage_bytes * 2);
         if (err != cudaSuccess) return cuda_fail(err, "allocating the work list");
-        plan->cap_work = num_work * 2;
+        plan->cap_device = stage_bytes * 2;
     }
-    std::memcpy(plan->h_stage, srcs.data(), src_bytes);
-    int2 *work = reinterpret_cast<int2 *>(plan->h_stage + work_off);
+    unsigned char *hs = plan->h_stage;
+    std::memcpy(hs, srcs.data(), src_bytes);
+    int2 *work = reinterpret_cast<int2 *>(hs + work_off);
     size_t w = 0;
     for (int i = 0; i < num_sources; ++i) {
         const long tiles = (long)((sources[i].n - 2LL * sources[i].tdi_start + tile - 1) / tile);
         for (long t = 0; t < tiles; ++t) work[w++] = make_int2(i, (int)t);
     }
-    err = cudaMemcpyAsync(plan->d_sources, plan->h_stage, src_bytes, cudaMemcpyHostToDevice, st);
-    if (err == cudaSuccess)
-        err = cudaMemcpyAsync(plan->d_work, work, sizeof(int2) * num_work, cudaMemcpyHostToDevice,
-                              st);
+    if (gb) {
+        flr::GbParams *gp = reinterpret_cast<flr::GbParams *>(hs + gb_off);
+        for (int i = 0; i < num_sources; ++i)
+            gp[i] = flr::GbParams{gb[i].A, gb[i].f, gb[i].fdot, gb[i].iota, gb[i].phi0, gb[i].psi};
+        std::memcpy(hs + cs_off, chunk_start.data(), sizeof(long) * srcs.size());
+    }
+    err = cudaMemcpyAsync(plan->d_stage, hs, stage_bytes, cudaMemcpyHostToDevice, st);
     if (err == cudaSuccess) err = cudaEventRecord(plan->stage_free, st);
     if (err != cudaSuccess) return cuda_fail(err, "copying the work list");
     plan->stage_pending = true;
 
+    const flr::FusedSource *d_src = reinterpret_cast<const flr::FusedSource *>(plan->d_stage);
+    if (gb) {
+        err = flr::launch_gb_waveforms(
+            d_src, reinterpret_cast<const flr::GbParams *>(plan->d_stage + gb_off),
+            reinterpret_cast<const long *>(plan->d_stage + cs_off), num_sources, num_chunks,
+            plan->base.dt, plan->sms * 8, st);
+        if (err != cudaSuccess) return cuda_fail(err, "launching the waveform kernel");
+    }
     flr::FusedArgs a = plan->base;
-    a.sources = plan->d_sources;
-    a.work = plan->d_work;
+    a.sources = d_src;
+    a.work = reinterpret_cast<const int2 *>(plan->d_stage + work_off);
     a.num_work = (int)num_work;
     a.chan = chan;
     const int grid = (int)std::min<size_t>(num_work, (size_t)plan->grid_max);
     err = flr::launch_fused(plan->mixed, a, grid, plan->smem, st);
     if (err != cudaSuccess) return cuda_fail(err, "launching the fused kernel");
     return FLR_OK;
+}
+
+int flr_batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int num_sources,
+                  int chan, void *stream) {
+    return batch_run(plan, sources, num_sources, nullptr, chan, stream);
+}
+
+int flr_batch_run_gb(flr_batch_plan *plan, const flr_batch_source *sources,
+                     const flr_gb_params *params, int num_sources, int chan, void *stream) {
+    if (num_sources > 0 && !params)
+        return fail(FLR_E_INVALID_ARGUMENT, "params must not be NULL");
+    return batch_run(plan, sources, num_sources, params, chan, stream);
 }
 
 }  // extern "C"

@@ -67,6 +67,16 @@ struct FusedArgs {
     int chan;                  // FusedChan
 };
 
+// Galactic-binary parameters of one source (on-device waveform generation).
+struct GbParams {
+    double A, f, fdot, iota, phi0, psi;
+};
+
+long gb_waveform_chunks(long n);
+cudaError_t launch_gb_waveforms(const FusedSource *src, const GbParams *par,
+                                const long *chunk_start, int num_sources, long num_chunks,
+                                double dt, int grid, cudaStream_t stream);
+
 size_t fused_smem_bytes(bool mixed, int win_max, int y_max);
 cudaError_t fused_configure(bool mixed, size_t smem_bytes, int *blocks_per_sm);
 cudaError_t launch_fused(bool mixed, const FusedArgs &a, int grid, size_t smem_bytes,

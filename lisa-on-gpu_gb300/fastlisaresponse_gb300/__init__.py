@@ -11,6 +11,7 @@ from ._lib import FLRError, describe_status, library_path
 from .batch import BatchedResponseTDI
 from .binding import LISAResponseWrap, LISAResponseWrapGPU, OrbitsWrap, OrbitsWrapGPU_responselisa
 from .orbits import EqualArmlengthOrbits, KeplerianOrbits, Orbits
+from .serve import Request, ResponseServer
 from .response import (ResponseWrapper, lagrange_tables, pyResponseTDI, sky_basis,
                        tdi_unit_tables)
 from .utils import AET, get_overlap
@@ -23,5 +24,5 @@ __all__ = [
     "LISAResponseWrap", "LISAResponseWrapGPU", "Orbits", "OrbitsWrap",
     "OrbitsWrapGPU_responselisa", "ResponseWrapper", "build", "describe_status",
     "gb_waveform", "get_overlap", "lagrange_tables", "library_path", "needs_build",
-    "pyResponseTDI", "sky_basis", "tdi_unit_tables", "time_grid",
+    "pyResponseTDI", "Request", "ResponseServer", "sky_basis", "tdi_unit_tables", "time_grid",
 ]

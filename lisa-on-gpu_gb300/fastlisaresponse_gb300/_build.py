@@ -33,6 +33,7 @@ SOURCES = {
     "flr_noalloc.cu": ["--fmad=false"],
     "flr_fused.cu": ["--fmad=false"],
     "flr_batch.cu": [],
+    "flr_waveform.cu": ["--fmad=false"],
 }
 
 _lock = threading.Lock()

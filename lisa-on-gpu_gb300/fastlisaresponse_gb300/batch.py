@@ -52,6 +52,11 @@ class _TdiUnits(ctypes.Structure):
                 ("num_combos", ctypes.c_int)]
 
 
+class _GbParams(ctypes.Structure):
+    _fields_ = [("A", ctypes.c_double), ("f", ctypes.c_double), ("fdot", ctypes.c_double),
+                ("iota", ctypes.c_double), ("phi0", ctypes.c_double), ("psi", ctypes.c_double)]
+
+
 class _Source(ctypes.Structure):
     _fields_ = [("h", ctypes.c_void_p),
                 ("out", ctypes.c_void_p),
@@ -89,6 +94,9 @@ def _plan_fns():
     lib.flr_batch_plan_info.restype = i
     lib.flr_batch_run.argtypes = [p, ctypes.POINTER(_Source), i, i, p]
     lib.flr_batch_run.restype = i
+    lib.flr_batch_run_gb.argtypes = [p, ctypes.POINTER(_Source), ctypes.POINTER(_GbParams), i, i,
+                                     p]
+    lib.flr_batch_run_gb.restype = i
     return lib
 
 
@@ -221,6 +229,55 @@ class BatchedResponseTDI:
         _lib.check(rc)
         self._last_inputs = hs  # keep the inputs alive until the next call
         return outs
+
+    def run_gb(self, params, lengths, lam, beta, t0=0.0, tdi_set=0, h=None, out=None,
+               stream=None):
+        """Generate galactic-binary waveforms on the device and evaluate them.
+
+        Args:
+            params: (num_sources, 6) array of (A, f, fdot, iota, phi0, psi).
+            lengths: samples per source.
+            lam, beta, t0, tdi_set: as for __call__ (scalars broadcast).
+            h: optional list of complex128 CUDA buffers of the given lengths
+                that receive the waveforms (allocated when omitted).
+            out: optional list of zeroed (3, n) float64 CUDA tensors.
+        Returns:
+            (outs, hs): the TDI channels and the generated waveforms.
+        """
+        params = np.asarray(params, dtype=np.float64).reshape(-1, 6)
+        ns = len(params)
+        lengths = np.broadcast_to(np.asarray(lengths, dtype=np.int64), (ns,))
+        lam = np.broadcast_to(np.asarray(lam, dtype=np.float64), (ns,))
+        beta = np.broadcast_to(np.asarray(beta, dtype=np.float64), (ns,))
+        t0 = np.broadcast_to(np.asarray(t0, dtype=np.float64), (ns,))
+        sets = np.broadcast_to(np.asarray(tdi_set, dtype=np.int64), (ns,))
+        dev = self.device
+        hs = list(h) if h is not None else [
+            torch.empty(int(n), dtype=torch.complex128, device=dev) for n in lengths]
+        outs = list(out) if out is not None else [
+            torch.zeros((3, int(n)), dtype=torch.float64, device=dev) for n in lengths]
+        srcs = (_Source * ns)()
+        gbs = (_GbParams * ns)()
+        for i in range(ns):
+            n = int(lengths[i])
+            if hs[i].numel() != n or hs[i].dtype != torch.complex128 or not hs[i].is_cuda:
+                raise ValueError(f"h[{i}] must be a complex128 CUDA buffer of {n} samples")
+            if tuple(outs[i].shape) != (3, n) or outs[i].dtype != torch.float64:
+                raise ValueError(f"out[{i}] must be a (3, {n}) float64 tensor")
+            k, u, v = sky_basis(float(lam[i]), float(beta[i]))
+            srcs[i] = _Source(hs[i].data_ptr(), outs[i].data_ptr(), n, self.projections_start_ind,
+                              self.tdi_start_ind, float(t0[i]), (ctypes.c_double * 3)(*k),
+                              (ctypes.c_double * 3)(*u), (ctypes.c_double * 3)(*v),
+                              int(sets[i]), 0)
+            gbs[i] = _GbParams(*[float(x) for x in params[i]])
+        if stream is None:
+            stream = torch.cuda.current_stream(dev)
+        lib = _plan_fns()
+        with torch.cuda.device(dev):
+            rc = lib.flr_batch_run_gb(self._plan, srcs, gbs, ns, CHANNELS[self.tdi_chan],
+                                      ctypes.c_void_p(stream.cuda_stream))
+        _lib.check(rc)
+        return outs, hs
 
     def status(self, reset: bool = False) -> int:
         """Kernel status bits (see include/flr_gb300.h; 0x10 = a staging copy
