@@ -332,6 +332,85 @@ def run_batch_section(args, device, peaks):
     return res
 
 
+def run_serving_section(args, device):
+    """Open-loop Poisson request streams against ResponseServer: saturation
+    throughput, then p50/p99 latency at rates below it."""
+    import threading
+
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+
+    dt = 10.0
+    count = args.serve_requests
+    rng = np.random.default_rng(5)
+    lengths = np.exp(rng.uniform(np.log(2**14), np.log(2**22), count)).astype(np.int64)
+    p = flr.waveforms.draw_gb_parameters(rng, count)
+    params = [(p["A"][i], p["f"][i], p["fdot"][i], p["iota"][i], p["phi0"][i], p["psi"][i],
+               p["lam"][i], p["beta"][i]) for i in range(count)]
+    sets = rng.integers(0, 2, count)
+    orb = flr.EqualArmlengthOrbits(t_max=(math.floor(lengths.max() * dt / 1e4) + 3) * 1e4)
+    out = {"workload": "open-loop Poisson requests: lengths log-uniform 2^14..2^22 at dt = 10 s, "
+                       "1st/2nd-gen TDI 50/50, galactic-binary parameters drawn as in the "
+                       "batching configuration, waveforms generated on the device, mixed "
+                       "precision, 160 GB admission budget, 2 streams",
+           "requests_per_rate": count, "mean_samples": float(lengths.mean())}
+
+    # batched throughput of the same requests in one launch pair (reference point)
+    bat = flr.BatchedResponseTDI(1 / dt, tdi=["1st generation", "2nd generation"], orbits=orb,
+                                 precision="mixed", force_backend=device)
+    prm = np.asarray([q[:6] for q in params])
+    lam = [q[6] for q in params]
+    beta = [q[7] for q in params]
+    bat.run_gb(prm[:4], lengths[:4], lam[:4], beta[:4], tdi_set=sets[:4])  # warm-up
+    torch.cuda.synchronize(device)
+    e0, e1 = _events()
+    e0.record()
+    outs, hs = bat.run_gb(prm, lengths, lam, beta, tdi_set=sets)
+    e1.record()
+    torch.cuda.synchronize(device)
+    del outs, hs
+    secs = e0.elapsed_time(e1) * 1e-3
+    n_out = int(sum(int(n) - 2000 for n in lengths))
+    out["batched_throughput_samples_per_s"] = n_out / secs
+    del bat
+
+    def run(rate):
+        with flr.ResponseServer(1 / dt, orbits=orb, num_streams=2, force_backend=device) as srv:
+            srv.submit(params[0], int(lengths[0]), int(sets[0])).result(timeout=60)  # warm-up
+            srv.completed.clear()
+            arrivals = (np.cumsum(rng.exponential(1.0 / rate, count)) if rate
+                        else np.zeros(count))
+
+            def client():
+                t_start = time.perf_counter()
+                for i in range(count):
+                    delay = t_start + arrivals[i] - time.perf_counter()
+                    if delay > 0:
+                        time.sleep(delay)
+                    srv.submit(params[i], int(lengths[i]), int(sets[i]))
+
+            th = threading.Thread(target=client)
+            th.start()
+            th.join()
+            while len(srv.completed) < count:
+                time.sleep(0.005)
+            st = srv.stats()
+        return st
+
+    sat = run(None)
+    out["saturation"] = sat
+    cap = sat["throughput_requests_per_s"]
+    out["rates"] = []
+    for frac in (0.5, 0.8, 0.9):
+        st = run(frac * cap)
+        st["offered_requests_per_s"] = frac * cap
+        st["fraction_of_batched_throughput"] = (st["throughput_samples_per_s"] /
+                                                out["batched_throughput_samples_per_s"])
+        out["rates"].append(st)
+    return out
+
+
 def run_ours(args, rank, world, device):
     import torch
 
@@ -534,6 +613,8 @@ def run_ours(args, rank, world, device):
     }
     if args.batch_sources > 0 and world == 1:
         result["batched"] = run_batch_section(args, device, peaks)
+    if args.serve_requests > 0 and world == 1:
+        result["serving"] = run_serving_section(args, device)
     return result
 
 
@@ -584,6 +665,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-sources", type=int, default=256,
                     help="sources in the config-3-shaped batch section (0 = skip)")
+    ap.add_argument("--serve-requests", type=int, default=1000,
+                    help="requests per arrival rate in the serving section (0 = skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
 
