@@ -655,6 +655,34 @@ def run_reference(args):
     return line
 
 
+def run_profile_batch(spec: str) -> None:
+    """Small batched case for ncu captures: 16 galactic binaries x 2^18
+    samples at dt = 10 s, 2nd-gen TDI, order 25; spec = "<fp64|mixed>:<equal|kepler>".
+    Two calls of the batch (the capture takes the first)."""
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+
+    prec, kind = spec.split(":")
+    dev = torch.device("cuda", 0)
+    dt, ns, n = 10.0, 16, 2**18
+    rng = np.random.default_rng(5)
+    t_max = (n * dt // 1e4 + 3) * 1e4
+    orb = flr.EqualArmlengthOrbits(t_max=t_max) if kind == "equal" else \
+        flr.KeplerianOrbits(t_max=t_max)
+    p = flr.waveforms.draw_gb_parameters(rng, ns)
+    t = torch.arange(n, dtype=torch.float64, device=dev) * dt
+    hs = [flr.gb_waveform(p["A"][i], p["f"][i], p["fdot"][i], p["iota"][i], p["phi0"][i],
+                          p["psi"][i], t) for i in range(ns)]
+    bat = flr.BatchedResponseTDI(1 / dt, order=25, tdi="2nd generation", orbits=orb,
+                                 precision=prec)
+    for _ in range(2):
+        bat(hs, p["lam"], p["beta"])
+    torch.cuda.synchronize()
+    assert bat.status() == 0
+    print(json.dumps({"profile_batch": spec, "plan": bat.plan_info}))
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -667,7 +695,15 @@ def main():
                     help="sources in the config-3-shaped batch section (0 = skip)")
     ap.add_argument("--serve-requests", type=int, default=1000,
                     help="requests per arrival rate in the serving section (0 = skip)")
+    ap.add_argument("--profile-batch", default=None, metavar="PREC:ORBIT",
+                    help="run only the small batched profiling case (fp64|mixed:equal|kepler)")
     args = ap.parse_args()
+    if args.profile_batch:
+        import fastlisaresponse_gb300 as flr
+
+        flr.build()
+        run_profile_batch(args.profile_batch)
+        return
     args.warmup = max(args.warmup, 0)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
