@@ -278,37 +278,42 @@ def _rel_l2_rows(got, want):
     return worst
 
 
-def _config3_sources(count, seed, dt, device):
+def _config3_sources(count, seed, dt, device, rank=0, world=1):
     """Sources drawn like the batching configuration: lengths log-uniform in
     2^15..2^22 samples, f log-U 1e-4..1e-2 Hz, fdot log-U 1e-18..1e-13,
-    A log-U 1e-23..1e-21, isotropic angles; waveforms generated on the device."""
+    A log-U 1e-23..1e-21, isotropic angles; waveforms generated on the device
+    for this rank's shard only (sources balanced over ranks by samples)."""
     import torch
 
     from fastlisaresponse_gb300 import waveforms as wf
+    from fastlisaresponse_gb300.dist import shard_by_samples
 
     rng = np.random.default_rng(seed)
     lengths = np.exp(rng.uniform(np.log(2**15), np.log(2**22), count)).astype(np.int64)
     p = wf.draw_gb_parameters(rng, count)
+    mine = shard_by_samples(lengths, rank, world)
     hs = []
-    for i, n in enumerate(lengths):
-        t = torch.arange(int(n), dtype=torch.float64, device=device) * dt
+    for i in mine:
+        t = torch.arange(int(lengths[i]), dtype=torch.float64, device=device) * dt
         hs.append(wf.gb_waveform(p["A"][i], p["f"][i], p["fdot"][i], p["iota"][i],
                                  p["phi0"][i], p["psi"][i], t))
-    return lengths, hs, p["lam"], p["beta"]
+    return lengths, mine, hs, p["lam"][mine], p["beta"][mine]
 
 
-def run_batch_section(args, device, peaks):
-    """Config-3-shaped batch: mixed vs FP64 fused kernels, same sources."""
-    import torch
-
+def run_batch_section(args, device, peaks, rank=0, world=1):
+    """Config-3-shaped batch: mixed vs FP64 fused kernels, same sources;
+    under torchrun the sources are sharded over the ranks (no collective on
+    the data path; the job time is the slowest rank's)."""
     import fastlisaresponse_gb300 as flr
+    from fastlisaresponse_gb300.dist import max_over_ranks
 
     dt = 10.0
-    lengths, hs, lam, beta = _config3_sources(args.batch_sources, seed=3, dt=dt, device=device)
+    lengths, mine, hs, lam, beta = _config3_sources(args.batch_sources, seed=3, dt=dt,
+                                                    device=device, rank=rank, world=world)
     orb = flr.EqualArmlengthOrbits(t_max=(math.floor(lengths.max() * dt / 1e4) + 3) * 1e4)
     n_out = int(sum(int(n) - 2 * int(T_BUFFER / dt) for n in lengths))
     res = {"sources": int(args.batch_sources), "samples": int(lengths.sum()),
-           "output_samples": n_out,
+           "output_samples": n_out, "sources_per_rank": len(mine),
            "workload": "config-3-shaped batch: lengths log-uniform 2^15..2^22 at dt = 10 s, "
                        "f log-U 1e-4..1e-2 Hz, equal-arm orbits, 2nd-gen TDI XYZ, order 25"}
     outs = {}
@@ -320,15 +325,15 @@ def run_batch_section(args, device, peaks):
         def step():
             holder["o"] = bat(hs, lam, beta)
 
-        secs = _timed(step, steps, 1, device)
+        secs = max_over_ranks([_timed(step, steps, 1, device)], device=device)[0]
         assert bat.status() == 0, flr.describe_status(bat.status())
         outs[prec] = holder["o"]
         res[prec] = {"value": n_out * steps / secs, "ms_per_step": 1e3 * secs / steps,
                      "steps": steps, "plan": bat.plan_info}
         del bat
     res["speedup_mixed_over_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
-    res["max_rel_l2_mixed_vs_fp64"] = max(_rel_l2_rows(a, b) for a, b in
-                                          zip(outs["mixed"], outs["fp64"]))
+    res["max_rel_l2_mixed_vs_fp64"] = max_over_ranks(
+        [max(_rel_l2_rows(a, b) for a, b in zip(outs["mixed"], outs["fp64"]))], device=device)[0]
     return res
 
 
@@ -505,10 +510,9 @@ def run_ours(args, rank, world, device):
     e2e_elapsed = _timed(e2e_step, args.steps, args.warmup, device)
     barrier()
 
-    times = torch.tensor([elapsed, e2e_elapsed], dtype=torch.float64, device=device)
-    if world > 1:
-        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
-    elapsed, e2e_elapsed = float(times[0]), float(times[1])
+    from fastlisaresponse_gb300.dist import max_over_ranks
+
+    elapsed, e2e_elapsed = max_over_ranks([elapsed, e2e_elapsed], device=device)
 
     # --- rooflines
     tables = resp.tdi_tables_host
@@ -611,8 +615,8 @@ def run_ours(args, rank, world, device):
         "roofline": roofline,
         "clocks": clock_info,
     }
-    if args.batch_sources > 0 and world == 1:
-        result["batched"] = run_batch_section(args, device, peaks)
+    if args.batch_sources > 0:
+        result["batched"] = run_batch_section(args, device, peaks, rank, world)
     if args.serve_requests > 0 and world == 1:
         result["serving"] = run_serving_section(args, device)
     return result

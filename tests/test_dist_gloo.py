@@ -1,0 +1,63 @@
+"""Multi-rank logic on the CPU: two gloo ranks shard a batch of sources and
+reduce their timings (the path bench.py takes under torchrun)."""
+
+import os
+import socket
+
+import numpy as np
+import pytest
+
+from fastlisaresponse_gb300.dist import max_over_ranks, shard_by_samples
+
+
+def test_shards_partition_and_balance():
+    rng = np.random.default_rng(0)
+    lengths = np.exp(rng.uniform(np.log(2**15), np.log(2**22), 2048)).astype(int)
+    for world in (1, 2, 4, 8):
+        shards = [shard_by_samples(lengths, r, world) for r in range(world)]
+        flat = sorted(i for s in shards for i in s)
+        assert flat == list(range(len(lengths)))
+        loads = [int(lengths[s].sum()) for s in shards]
+        assert max(loads) - min(loads) <= int(lengths.max())
+    with pytest.raises(ValueError):
+        shard_by_samples([1, 2], 2, 2)
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, lengths, q):
+    import torch.distributed as td
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    td.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        mine = shard_by_samples(lengths, rank, world)
+        work = float(sum(lengths[i] for i in mine))
+        reduced = max_over_ranks([work, float(rank)])
+        q.put((rank, mine, work, reduced))
+    finally:
+        td.destroy_process_group()
+
+
+def test_two_gloo_ranks_shard_and_reduce():
+    import torch.multiprocessing as mp
+
+    lengths = [int(x) for x in np.random.default_rng(1).integers(1000, 100000, 37)]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, lengths, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    results = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    (r0, s0, w0, red0), (r1, s1, w1, red1) = results
+    assert sorted(s0 + s1) == list(range(len(lengths)))
+    assert red0 == red1 == [max(w0, w1), 1.0]
