@@ -216,6 +216,14 @@ typedef struct {
     double k[3], u[3], v[3];/* propagation direction and polarisation basis */
     int tdi_set;            /* index of the plan's TDI unit set */
     int reserved;
+    /* Optional diagnostics (NULL = off), written for samples [tdi_start, n - tdi_start):
+     *   y_out [6][n] the link streams (y_gw) the TDI stage used;
+     *   d_rec_out, d_em_out [6][n] receiver / emitter integer delays (both or neither);
+     *   d_tdi_out [num_units][n] integer TDI delays, units in the set's given order. */
+    double *y_out;
+    int *d_rec_out;
+    int *d_em_out;
+    int *d_tdi_out;
 } flr_batch_source;
 
 typedef struct flr_batch_plan flr_batch_plan;

@@ -166,6 +166,7 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
                 return fail(FLR_E_INVALID_ARGUMENT, "channels must be 0, 1 or 2");
             s.unit_start[u] = st;
             s.unit_len[u] = ln;
+            s.orig_unit[u] = src_u;
             s.base_slot[u] = slot_of(orbits, in.tdi_base_link[src_u]);
             if (s.base_slot[u] < 0)
                 return fail(FLR_E_INVALID_ARGUMENT, "TDI base link is not an orbit link");
@@ -307,6 +308,7 @@ static int batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int 
     size_t num_work = 0;
     long num_chunks = 0;
     std::vector<long> chunk_start(num_sources);
+    bool diag = false;
     for (int i = 0; i < num_sources; ++i) {
         const flr_batch_source &s = sources[i];
         if (!s.h || !s.out || s.n < 2 || s.projections_start < 0 ||
@@ -333,6 +335,13 @@ static int batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int 
         }
         d.tdi_set = s.tdi_set;
         d.pad = 0;
+        d.y_out = s.y_out;
+        d.d_rec_out = s.d_rec_out;
+        d.d_em_out = s.d_em_out;
+        d.d_tdi_out = s.d_tdi_out;
+        diag = diag || s.y_out || s.d_rec_out || s.d_tdi_out;
+        if ((s.d_rec_out == nullptr) != (s.d_em_out == nullptr))
+            return fail(FLR_E_INVALID_ARGUMENT, "d_rec_out and d_em_out go together");
         num_work += (size_t)((s.n - 2LL * s.tdi_start + tile - 1) / tile);
         chunk_start[i] = num_chunks;
         num_chunks += flr::gb_waveform_chunks((long)s.n);
@@ -405,7 +414,7 @@ static int batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int 
     a.num_work = (int)num_work;
     a.chan = chan;
     const int grid = (int)std::min<size_t>(num_work, (size_t)plan->grid_max);
-    err = flr::launch_fused(plan->mixed, a, grid, plan->smem, st);
+    err = flr::launch_fused(plan->mixed, diag, a, grid, plan->smem, st);
     if (err != cudaSuccess) return cuda_fail(err, "launching the fused kernel");
     return FLR_OK;
 }

@@ -357,7 +357,7 @@ __device__ __forceinline__ df::f2 df_interp_real(const float2 *y, int d, df::f2 
 
 // -------------------------------------------------------------- the kernel ----
 
-template <bool kMixed>
+template <bool kMixed, bool kDiag>
 __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     const Layout lay = layout(kMixed, a.win_max, a.y_max);
@@ -518,6 +518,11 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
             const double t = t0 + (double)j * a.dt;
             if (kMixed) {
                 const MixedDelays g = link_delays_mixed(a.orb, a.inv_orbit_dt, slot, t, t0, a.fs, k);
+                const bool own = (j >= o0 && j < o1);  // this tile's outputs: diagnostics
+                if (kDiag && own && src.d_rec_out) {
+                    src.d_rec_out[(long)slot * n + j] = g.d_rec;
+                    src.d_em_out[(long)slot * n + j] = g.d_em;
+                }
                 const long lo = (long)min(g.d_rec, g.d_em) - (h - 1);
                 const long hi = (long)max(g.d_rec, g.d_em) + h;
                 const df::f2 e_r = df::from_double(g.e_rec), e_e = df::from_double(g.e_em);
@@ -542,8 +547,15 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
                 df::f2 yv = df::add(df::mul(dre, pr.xi_p), df::mul(dim, pr.xi_c));
                 yv = df::mul(yv, pr.pre);
                 y32[slot * a.y_max + jj] = make_float2(yv.hi, yv.lo);
+                if (kDiag && own && src.y_out)
+                    src.y_out[(long)slot * n + j] = df::to_double(yv) / scale;
             } else {
                 const LinkGeometry g = link_geometry(a.orb, slot, t, t0, a.fs, k, u, v);
+                const bool own = (j >= o0 && j < o1);
+                if (kDiag && own && src.d_rec_out) {
+                    src.d_rec_out[(long)slot * n + j] = g.d_rec;
+                    src.d_em_out[(long)slot * n + j] = g.d_em;
+                }
                 const long lo = (long)min(g.d_rec, g.d_em) - (h - 1);
                 const long hi = (long)max(g.d_rec, g.d_em) + h;
                 double A_r, A_e, out;
@@ -571,6 +583,7 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
                     out = qnan();
                 }
                 y64[slot * a.y_max + jj] = out;
+                if (kDiag && own && src.y_out) src.y_out[(long)slot * n + j] = out;
             }
         }
         __syncthreads();
@@ -616,6 +629,7 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
                 } else {
                     split_delay(delay, t0, a.fs, d, eps);
                 }
+                if (kDiag && src.d_tdi_out) src.d_tdi_out[(long)set->orig_unit[unit] * n + i] = d;
                 const int b = set->base_slot[unit];
                 const long lo = (long)d - (h - 1), hi = (long)d + h;
                 if (lo < ya || hi >= yb) {
@@ -679,23 +693,31 @@ size_t fused_smem_bytes(bool mixed, int win_max, int y_max) {
     return layout(mixed, win_max, y_max).total;
 }
 
-cudaError_t fused_configure(bool mixed, size_t smem_bytes, int *blocks_per_sm) {
-    const void *fn = mixed ? reinterpret_cast<const void *>(fused_kernel<true>)
-                           : reinterpret_cast<const void *>(fused_kernel<false>);
-    cudaError_t err =
-        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
-    if (err != cudaSuccess) return err;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, kThreads, smem_bytes);
+static const void *fused_fn(bool mixed, bool diag) {
+    if (diag)
+        return mixed ? reinterpret_cast<const void *>(fused_kernel<true, true>)
+                     : reinterpret_cast<const void *>(fused_kernel<false, true>);
+    return mixed ? reinterpret_cast<const void *>(fused_kernel<true, false>)
+                 : reinterpret_cast<const void *>(fused_kernel<false, false>);
 }
 
-cudaError_t launch_fused(bool mixed, const FusedArgs &a, int grid, size_t smem_bytes,
+cudaError_t fused_configure(bool mixed, size_t smem_bytes, int *blocks_per_sm) {
+    for (bool diag : {true, false}) {
+        cudaError_t err = cudaFuncSetAttribute(fused_fn(mixed, diag),
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)smem_bytes);
+        if (err != cudaSuccess) return err;
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fused_fn(mixed, false),
+                                                         kThreads, smem_bytes);
+}
+
+cudaError_t launch_fused(bool mixed, bool diag, const FusedArgs &a, int grid, size_t smem_bytes,
                          cudaStream_t stream) {
     if (a.num_work <= 0) return cudaSuccess;
-    if (mixed)
-        fused_kernel<true><<<grid, kThreads, smem_bytes, stream>>>(a);
-    else
-        fused_kernel<false><<<grid, kThreads, smem_bytes, stream>>>(a);
-    return cudaGetLastError();
+    void *args[] = {const_cast<FusedArgs *>(&a)};
+    return cudaLaunchKernel(fused_fn(mixed, diag), dim3(grid), dim3(kThreads), args, smem_bytes,
+                            stream);
 }
 
 }  // namespace flr

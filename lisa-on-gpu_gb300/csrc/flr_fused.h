@@ -23,6 +23,11 @@ struct FusedSource {
     double k[3], u[3], v[3];
     int tdi_set;        // index into the TDI table sets
     int pad;
+    // optional diagnostics (NULL = off), written for the output samples [ts, n - ts):
+    double *y_out;      // [6][n] link streams
+    int *d_rec_out;     // [6][n] receiver integer delays
+    int *d_em_out;      // [6][n] emitter integer delays
+    int *d_tdi_out;     // [num_units][n] TDI integer delays, in the caller's unit order
 };
 
 // TDI unit tables with link numbers already mapped to link slots.
@@ -41,6 +46,7 @@ struct FusedTdiSet {
     // would compute itself (same subtractions in the same order).
     int delay_len[kFusedMaxUnits];
     int prefix_keep[kFusedMaxUnits];
+    int orig_unit[kFusedMaxUnits];    // position of the unit in the caller's table
     int delay_slot[kFusedMaxUnits][kFusedMaxDepth];
     int combo_slot[kFusedMaxCombos];  // -1: no delay
 };
@@ -79,7 +85,8 @@ cudaError_t launch_gb_waveforms(const FusedSource *src, const GbParams *par,
 
 size_t fused_smem_bytes(bool mixed, int win_max, int y_max);
 cudaError_t fused_configure(bool mixed, size_t smem_bytes, int *blocks_per_sm);
-cudaError_t launch_fused(bool mixed, const FusedArgs &a, int grid, size_t smem_bytes,
+// diag: the instance that writes the FusedSource diagnostics (more registers).
+cudaError_t launch_fused(bool mixed, bool diag, const FusedArgs &a, int grid, size_t smem_bytes,
                          cudaStream_t stream);
 
 }  // namespace flr

@@ -68,7 +68,11 @@ class _Source(ctypes.Structure):
                 ("u", ctypes.c_double * 3),
                 ("v", ctypes.c_double * 3),
                 ("tdi_set", ctypes.c_int),
-                ("reserved", ctypes.c_int)]
+                ("reserved", ctypes.c_int),
+                ("y_out", ctypes.c_void_p),
+                ("d_rec_out", ctypes.c_void_p),
+                ("d_em_out", ctypes.c_void_p),
+                ("d_tdi_out", ctypes.c_void_p)]
 
 
 def _combinations(spec):
@@ -184,7 +188,7 @@ class BatchedResponseTDI:
             pass
 
     def __call__(self, h: Sequence, lam, beta, t0=0.0, tdi_set=0, out: Optional[Sequence] = None,
-                 stream=None):
+                 stream=None, diagnostics: bool = False):
         """Evaluate the batch.
 
         Args:
@@ -196,9 +200,13 @@ class BatchedResponseTDI:
             tdi_set: TDI set index per source (scalar broadcasts).
             out: optional list of (3, n) float64 CUDA tensors to write into
                 (zeroed by the caller); allocated (zeros) when omitted.
+            diagnostics: also return, per source, the link streams and the
+                integer delays the kernel used (for the output samples).
         Returns:
             list of (3, n) tensors: rows X, Y, Z (or A, E, T / A, E and a
             zero third row); samples within t_buffer of either end are zero.
+            With diagnostics, (outs, diags) where diags[i] is a dict of
+            "y" (6, n), "d_rec" / "d_em" (6, n) and "d_tdi" (units, n).
         """
         ns = len(h)
         lam = np.broadcast_to(np.asarray(lam, dtype=np.float64), (ns,))
@@ -210,16 +218,27 @@ class BatchedResponseTDI:
         outs = list(out) if out is not None else [
             torch.zeros((3, len(x)), dtype=torch.float64, device=dev) for x in hs]
         srcs = (_Source * ns)()
+        diags = []
         for i in range(ns):
             n = len(hs[i])
             o = outs[i]
             if tuple(o.shape) != (3, n) or o.dtype != torch.float64 or not o.is_contiguous():
                 raise ValueError(f"out[{i}] must be a contiguous (3, {n}) float64 tensor")
             k, u, v = sky_basis(float(lam[i]), float(beta[i]))
+            ptrs = [None] * 4
+            if diagnostics:
+                nu = self.tdi_sets[int(sets[i])]["num_units"]
+                dg = {"y": torch.zeros((6, n), dtype=torch.float64, device=dev),
+                      "d_rec": torch.zeros((6, n), dtype=torch.int32, device=dev),
+                      "d_em": torch.zeros((6, n), dtype=torch.int32, device=dev),
+                      "d_tdi": torch.zeros((nu, n), dtype=torch.int32, device=dev)}
+                diags.append(dg)
+                ptrs = [dg["y"].data_ptr(), dg["d_rec"].data_ptr(), dg["d_em"].data_ptr(),
+                        dg["d_tdi"].data_ptr()]
             srcs[i] = _Source(hs[i].data_ptr(), o.data_ptr(), n, self.projections_start_ind,
                               self.tdi_start_ind, float(t0[i]), (ctypes.c_double * 3)(*k),
                               (ctypes.c_double * 3)(*u), (ctypes.c_double * 3)(*v),
-                              int(sets[i]), 0)
+                              int(sets[i]), 0, *ptrs)
         if stream is None:
             stream = torch.cuda.current_stream(dev)
         lib = _plan_fns()
@@ -228,7 +247,7 @@ class BatchedResponseTDI:
                                    ctypes.c_void_p(stream.cuda_stream))
         _lib.check(rc)
         self._last_inputs = hs  # keep the inputs alive until the next call
-        return outs
+        return (outs, diags) if diagnostics else outs
 
     def run_gb(self, params, lengths, lam, beta, t0=0.0, tdi_set=0, h=None, out=None,
                stream=None):

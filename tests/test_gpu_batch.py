@@ -100,3 +100,49 @@ def test_batch_mixed_accuracy(gpu_lib, order, gen):
             worst = max(worst, err)
             assert err <= MIXED_TOL, f"f={f[i]} channel {c}: rel L2 {err:.3e}"
     print(f"order {order} {gen}: worst rel L2 {worst:.3e}")
+
+
+@pytest.mark.parametrize("orbit_kind", ["equal", "kepler"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_indices_and_links_match_plain(gpu_lib, orbit_kind, precision):
+    """The integer delays the fused kernel uses (receiver, emitter, every TDI
+    unit) equal the plain path's bit for bit, in both flavours; the fp64 link
+    streams equal the plain y_gw bit for bit, the mixed ones to 1e-6 per link."""
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+
+    dt = 10.0
+    lengths = [6000, 23000]
+    orb = flr.EqualArmlengthOrbits(t_max=4e5) if orbit_kind == "equal" else \
+        flr.KeplerianOrbits(t_max=4e5)
+    hs, lam, beta, t0 = _sources(orb, dt, lengths, seed=5)
+    bat = flr.BatchedResponseTDI(1 / dt, order=25, tdi="2nd generation", orbits=orb,
+                                 precision=precision)
+    outs, diags = bat(hs, lam, beta, t0=t0, diagnostics=True)
+    ts = bat.tdi_start_ind
+    for i, n in enumerate(lengths):
+        r = flr.pyResponseTDI(1 / dt, n, order=25, tdi="2nd generation", orbits=orb)
+        r.get_projections(hs[i], lam[i], beta[i], t0=t0[i], t_buffer=1e4)
+        dev = r.device
+        tt = torch.as_tensor(t0[i] + np.arange(n) * r.dt, device=dev)
+        k, _, _ = flr.sky_basis(lam[i], beta[i])
+        d_rec = torch.zeros(6 * n, dtype=torch.int32, device=dev)
+        d_em = torch.zeros_like(d_rec)
+        r.cpp_response.response_delay_indices(d_rec, d_em, tt, torch.as_tensor(k, device=dev), n,
+                                              1 / dt, r.projections_start_ind)
+        d_tdi = torch.zeros(r.num_units * n, dtype=torch.int32, device=dev)
+        r.cpp_response.tdi_delay_indices(d_tdi, n, tt, r.unit_starts, r.unit_lengths,
+                                         r.tdi_link_combinations, r.num_units, 1 / dt, ts)
+        sl = slice(ts, n - ts)
+        dg = diags[i]
+        assert np.array_equal(_np(dg["d_rec"])[:, sl], _np(d_rec).reshape(6, n)[:, sl])
+        assert np.array_equal(_np(dg["d_em"])[:, sl], _np(d_em).reshape(6, n)[:, sl])
+        assert np.array_equal(_np(dg["d_tdi"])[:, sl], _np(d_tdi).reshape(r.num_units, n)[:, sl])
+        y_plain = _np(r.y_gw)[:, sl]
+        y_fused = _np(dg["y"])[:, sl]
+        if precision == "fp64":
+            assert np.array_equal(y_fused, y_plain)
+        else:
+            for link in range(6):
+                assert rel_l2(y_fused[link], y_plain[link]) <= MIXED_TOL
