@@ -337,6 +337,99 @@ def run_batch_section(args, device, peaks, rank=0, world=1):
     return res
 
 
+def _err_stats(got, want):
+    """Per-row relative L2 and max error (max |got - want| / max |want|)."""
+    import torch
+
+    d = got - want
+    num = torch.linalg.vector_norm(d, dim=1)
+    den = torch.linalg.vector_norm(want, dim=1)
+    mx = d.abs().amax(dim=1) / want.abs().amax(dim=1).clamp_min(1e-300)
+    return (num / den.clamp_min(1e-300)).cpu().numpy(), mx.cpu().numpy()
+
+
+def run_precision_section(args, device):
+    """Precision configuration: sources of 2^20 samples at dt = 10 s drawn as
+    in the batching configuration, Lagrange orders 25 and 45.  The mixed path
+    is compared with the FP64 fused path (bit-identical to the oracle and the
+    plain path) per link and per X/Y/Z channel, and its integer delay indices
+    (receiver, emitter, every TDI unit) with the FP64 path's, bit for bit."""
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+
+    dt, n = 10.0, 2**20
+    count = args.precision_sources
+    rng = np.random.default_rng(4)
+    p = flr.waveforms.draw_gb_parameters(rng, count)
+    orb = flr.EqualArmlengthOrbits(t_max=(math.floor(n * dt / 1e4) + 3) * 1e4)
+    t = torch.arange(n, dtype=torch.float64, device=device) * dt
+    chunk = 16
+    res = {"workload": f"{count} galactic binaries x 2^20 samples at dt = 10 s drawn as in the "
+                       "batching configuration, equal-arm orbits, 2nd-gen TDI XYZ",
+           "sources": count, "reference": "FP64 fused path (bit-identical to the oracle)"}
+    for order in (25, 45):
+        tb = 1e4 if order <= 25 else 2e4  # order 45 needs the longer garbage margin
+        plans = {prec: flr.BatchedResponseTDI(1 / dt, order=order, tdi="2nd generation",
+                                              orbits=orb, precision=prec, t_buffer=tb,
+                                              force_backend=device)
+                 for prec in ("fp64", "mixed")}
+        ts = plans["fp64"].tdi_start_ind
+        sl = slice(ts, n - ts)
+        link_l2, link_max, chan_l2, chan_max = [], [], [], []
+        mism = {"d_rec": 0, "d_em": 0, "d_tdi": 0}
+        secs = {"fp64": 0.0, "mixed": 0.0}
+        for c0 in range(0, count, chunk):
+            idx = range(c0, min(count, c0 + chunk))
+            hs = [flr.gb_waveform(p["A"][i], p["f"][i], p["fdot"][i], p["iota"][i],
+                                  p["phi0"][i], p["psi"][i], t) for i in idx]
+            lam, beta = p["lam"][list(idx)], p["beta"][list(idx)]
+            runs = {}
+            for prec, bat in plans.items():
+                bat(hs[:1], lam[:1], beta[:1])  # warm-up
+                holder = {}
+
+                def step():
+                    holder["o"] = bat(hs, lam, beta)
+
+                secs[prec] += _timed(step, 1, 0, device)
+                runs[prec] = (holder["o"], bat(hs, lam, beta, diagnostics=True)[1])
+                assert bat.status() == 0, flr.describe_status(bat.status())
+            for j in range(len(hs)):
+                (o64, d64), (omx, dmx) = [(runs[k][0][j], runs[k][1][j])
+                                          for k in ("fp64", "mixed")]
+                for key in mism:
+                    mism[key] += int((dmx[key][:, sl] != d64[key][:, sl]).sum().item())
+                a, b = _err_stats(dmx["y"][:, sl], d64["y"][:, sl])
+                link_l2.append(a)
+                link_max.append(b)
+                a, b = _err_stats(omx[:, sl], o64[:, sl])
+                chan_l2.append(a)
+                chan_max.append(b)
+            del runs, hs
+        link_l2, link_max = np.asarray(link_l2), np.asarray(link_max)
+        chan_l2, chan_max = np.asarray(chan_l2), np.asarray(chan_max)
+        n_out = count * (n - 2 * ts)
+        res[f"order_{order}"] = {
+            "t_buffer_s": tb,
+            "per_link": {str(k): {"rel_l2_max": float(link_l2[:, k].max()),
+                                  "rel_l2_median": float(np.median(link_l2[:, k])),
+                                  "max_err_max": float(link_max[:, k].max())}
+                         for k in range(6)},
+            "per_channel": {ch: {"rel_l2_max": float(chan_l2[:, k].max()),
+                                 "rel_l2_median": float(np.median(chan_l2[:, k])),
+                                 "max_err_max": float(chan_max[:, k].max())}
+                            for k, ch in enumerate("XYZ")},
+            "index_mismatches": mism,
+            "samples_per_s": {prec: n_out / s for prec, s in secs.items()},
+            "speedup_mixed_over_fp64": secs["fp64"] / secs["mixed"],
+        }
+        del plans
+        torch.cuda.empty_cache()
+    res["max_err_definition"] = "max |mixed - fp64| / max |fp64| per row"
+    return res
+
+
 def run_serving_section(args, device):
     """Open-loop Poisson request streams against ResponseServer: saturation
     throughput, then p50/p99 latency at rates below it."""
@@ -617,6 +710,8 @@ def run_ours(args, rank, world, device):
     }
     if args.batch_sources > 0:
         result["batched"] = run_batch_section(args, device, peaks, rank, world)
+    if args.precision_sources > 0 and world == 1:
+        result["precision"] = run_precision_section(args, device)
     if args.serve_requests > 0 and world == 1:
         result["serving"] = run_serving_section(args, device)
     return result
@@ -699,6 +794,8 @@ def main():
                     help="sources in the config-3-shaped batch section (0 = skip)")
     ap.add_argument("--serve-requests", type=int, default=1000,
                     help="requests per arrival rate in the serving section (0 = skip)")
+    ap.add_argument("--precision-sources", type=int, default=32,
+                    help="sources of 2^20 samples in the precision section (0 = skip)")
     ap.add_argument("--profile-batch", default=None, metavar="PREC:ORBIT",
                     help="run only the small batched profiling case (fp64|mixed:equal|kepler)")
     args = ap.parse_args()
