@@ -2,28 +2,34 @@
 """Benchmark of the LISA time-domain response + TDI on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload NAME] [--no-cpu-baseline]
+                    [--workload NAME] [--no-cpu-baseline] [--batch-sources S]
+                    [--precision-sources P] [--serve-requests R]
 
-One step = one pass of the hot path over one source: the six link
-projections (get_projections) and the TDI channels (get_tdi_delays).  The
-default workload is one galactic binary observed for 1 yr at dt = 5 s
-(6,311,629 samples) with flexing Keplerian orbits, 2nd-generation TDI XYZ and
-Lagrange order 25, all in float64, on the plain FP64 path (bit-identical to the
-reference's CPU arithmetic).
+One step = one pass of the hot path over one source: the six link projections
+and the TDI channels.  The default workload is one galactic binary observed
+for 1 yr at dt = 5 s (6,311,629 samples) with flexing Keplerian orbits,
+2nd-generation TDI XYZ and Lagrange order 25.  The headline runs it through
+the mixed-precision fused kernel (BatchedResponseTDI, autotuned tile; FP64
+delays and bit-exact indices, double-float taps); the plain FP64 drop-in path
+(pyResponseTDI, bit-identical to the reference's CPU arithmetic) is timed on
+the same source beside it.
 
 Printed on rank 0, one JSON line:
-  value      output samples/s with the input resident in HBM (device-timed with
-             CUDA events on the launching stream, max over ranks);
-  e2e        the same metric through pyResponseTDI with the input in pinned host
-             memory and X/Y/Z copied back to pinned host memory every step;
-  roofline   the dominant kernel's algorithmic FP64 operations per second
-             against the FP64-pipe peak measured at start-up by the probe
-             kernel (plus its HBM fraction against MEASURED_PEAKS.json);
-  cpu_baseline  the CPU oracle on a bounded slice of the same configuration.
+  value       output samples/s with the input resident in HBM (CUDA events
+              around each step, L2 flushed before each, max over ranks);
+  e2e         the same metric through BatchedResponseTDI with the input in
+              pinned host memory and X/Y/Z copied back to pinned host memory;
+  roofline    the fused kernel's FP64 index-path operations per second
+              against the FP64 FMA peak measured at start-up (and its HBM
+              fraction against MEASURED_PEAKS.json); plain_fp64.roofline the
+              same for the plain path's dominant kernel;
+  cpu_baseline  the C oracle on one host core, on a bounded slice;
+  batched / precision / serving  the batching, precision and serving
+              configurations (see their sections).
 With --impl reference the CPU implementation is timed instead (all host
 cores, one independent source per process) and printed with "impl":
-"reference".  Under torchrun every rank runs its own source (weak scaling);
-the reference arm runs on rank 0 only.
+"reference".  Under torchrun every rank runs its own source and its share of
+the batch (weak scaling); the reference arm runs on rank 0 only.
 """
 
 from __future__ import annotations
@@ -247,24 +253,45 @@ def _events():
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
 
+_FLUSH = {}
+
+
+def _flush_l2(device):
+    """Write 256 MB (twice the L2) so that a step starts with a cold L2."""
+    import torch
+
+    buf = _FLUSH.get(device)
+    if buf is None:
+        buf = _FLUSH[device] = torch.empty(2**25, dtype=torch.float64, device=device)
+    buf.fill_(1.0)
+
+
 def _timed(fn, steps, warmup, device, kernel_events=None):
-    """Run fn warmup + steps times; CUDA-event time of the steps [s]."""
+    """Run fn warmup + steps times; CUDA-event time of the steps [s].
+
+    Before each timed step the L2 is flushed and the stream is held for ~1 ms
+    (torch.cuda._sleep) while the host queues the step, so the events bracket
+    device work only; the step times are summed."""
     import torch
 
     for _ in range(warmup):
         fn()
     torch.cuda.synchronize(device)
-    e0, e1 = _events()
     if kernel_events is not None:
         kernel_events["on"] = True
-    e0.record()
+    pairs = []
     for _ in range(steps):
+        _flush_l2(device)
+        torch.cuda._sleep(2_000_000)
+        e0, e1 = _events()
+        e0.record()
         fn()
-    e1.record()
+        e1.record()
+        pairs.append((e0, e1))
     torch.cuda.synchronize(device)
     if kernel_events is not None:
         kernel_events["on"] = False
-    return e0.elapsed_time(e1) * 1e-3
+    return sum(a.elapsed_time(b) for a, b in pairs) * 1e-3
 
 
 def _rel_l2_rows(got, want):
@@ -319,7 +346,8 @@ def run_batch_section(args, device, peaks, rank=0, world=1):
     outs = {}
     for prec, steps in (("mixed", args.steps), ("fp64", 1)):
         bat = flr.BatchedResponseTDI(1 / dt, order=25, tdi="2nd generation", orbits=orb,
-                                     precision=prec)
+                                     precision=prec, tile="auto",
+                                     tune_lengths=[int(lengths[i]) for i in mine[:32]])
         holder = {}
 
         def step():
@@ -329,7 +357,7 @@ def run_batch_section(args, device, peaks, rank=0, world=1):
         assert bat.status() == 0, flr.describe_status(bat.status())
         outs[prec] = holder["o"]
         res[prec] = {"value": n_out * steps / secs, "ms_per_step": 1e3 * secs / steps,
-                     "steps": steps, "plan": bat.plan_info}
+                     "steps": steps, "plan": bat.plan_info, "tune": bat.tune}
         del bat
     res["speedup_mixed_over_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
     res["max_rel_l2_mixed_vs_fp64"] = max_over_ranks(
@@ -529,7 +557,8 @@ def run_ours(args, rank, world, device):
 
     # --- headline: mixed-precision fused path (BatchedResponseTDI, one source)
     bat = flr.BatchedResponseTDI(1.0 / dt, order=w["order"], tdi=w["tdi"], orbits=orb,
-                                 precision="mixed", force_backend=device)
+                                 precision="mixed", force_backend=device, tile="auto",
+                                 tune_lengths=[n])
     ev = {"on": False, "fused": []}
     run_fn = lib.flr_batch_run
 
@@ -694,8 +723,9 @@ def run_ours(args, rank, world, device):
                    "input_samples": n,
                    "path": "mixed-precision fused kernel (BatchedResponseTDI, one source); "
                            "integer delay indices bit-exact",
-                   "l2": "inputs larger than L2: h 16 B + XYZ 24 B per sample = "
-                         f"{40 * n / 1e6:.0f} MB per step"},
+                   "tile": bat.plan_info["tile"], "tile_tuning": bat.tune,
+                   "l2": "flushed before every timed step (256 MB write); h 16 B + XYZ "
+                         f"24 B per sample = {40 * n / 1e6:.0f} MB per step"},
         "accuracy": {"max_rel_l2_vs_plain_fp64": max_rel, "bound": 1e-6,
                      "per": "TDI channel, this run's outputs"},
         "plain_fp64": plain,

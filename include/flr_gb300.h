@@ -206,9 +206,9 @@ typedef struct {
 /* One source of a batch. */
 typedef struct {
     const void *h;          /* [n] complex128 h+ + i hx, device, 16-byte aligned */
-    double *out;            /* [3][n] float64, device: rows X,Y,Z (or A,E,T / A,E);
-                               samples [tdi_start, n - tdi_start) are written, the
-                               rest untouched (zero it to match the reference) */
+    double *out;            /* [3][n] float64, device: rows X,Y,Z (or A,E,T / A,E and
+                               a zero row); every sample is written, zeros outside
+                               [tdi_start, n - tdi_start) as in the reference */
     long long n;
     int projections_start;  /* link streams are zero outside [ps, n - ps) */
     int tdi_start;          /* first output sample (garbage margin) */
@@ -230,7 +230,8 @@ typedef struct flr_batch_plan flr_batch_plan;
 
 /* Plan for batches on `orbits`: Lagrange tables (device or host; copied),
  * 1..64 TDI unit sets, precision, tile = output samples per work item
- * (0 = 512).  Runs of one plan must be ordered on one stream. */
+ * (0 = 512).  A run on another stream than the previous run of the plan waits
+ * (on the device) for that run, whose staging buffer it reuses. */
 int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, double deps,
                           int num_A, const double *E_in, double sampling_frequency,
                           const flr_tdi_units *sets, int num_sets, int precision, int tile,
@@ -256,6 +257,30 @@ typedef struct {
  * t_i = t0 + i / fs.  One waveform launch and one fused launch per call. */
 int flr_batch_run_gb(flr_batch_plan *plan, const flr_batch_source *sources,
                      const flr_gb_params *params, int num_sources, int chan, void *stream);
+
+/*
+ * Batch graphs: the staging copy and the kernel launches of a run, captured
+ * once as a CUDA graph for up to `max_sources` sources and replayed by
+ * flr_batch_graph_launch.  The kernels take the number of tiles (and waveform
+ * chunks) of every source from the staged per-source prefix sums, so one graph
+ * runs batches of any lengths and of up to max_sources sources; everything
+ * per source (buffers, n, sky position, t0, TDI set, waveform parameters) is
+ * staged per launch.  Results are bit-identical to flr_batch_run /
+ * flr_batch_run_gb on the same sources.  Two pinned staging buffers alternate,
+ * so a launch can be prepared while the previous one runs; a launch on
+ * another stream than the previous one waits for it on the device.  Destroy
+ * the graphs of a plan before the plan.  No counterpart in the reference.
+ * flags: FLR_GRAPH_WAVEFORMS (generate waveforms as flr_batch_run_gb; params
+ * required at launch) | FLR_GRAPH_DIAGNOSTICS (allow the diagnostics fields).
+ */
+#define FLR_GRAPH_WAVEFORMS 0x1
+#define FLR_GRAPH_DIAGNOSTICS 0x2
+typedef struct flr_batch_graph flr_batch_graph;
+int flr_batch_graph_create(flr_batch_plan *plan, int max_sources, int flags, int chan,
+                           flr_batch_graph **out);
+int flr_batch_graph_launch(flr_batch_graph *graph, const flr_batch_source *sources,
+                           const flr_gb_params *params, int num_sources, void *stream);
+int flr_batch_graph_destroy(flr_batch_graph *graph);
 
 /*
  * Link projections without any device allocation.  No counterpart in the

@@ -5,9 +5,17 @@
 // tables, TDI unit sets, arithmetic, tile length -- derives the launch shape
 // (halo and window sizes, shared memory, persistent grid from the occupancy of
 // the kernel), and owns reusable device and pinned buffers for the per-run
-// source descriptors and work list.  A run flattens its sources into
-// (source, tile) work items, copies descriptors and items with one
-// asynchronous copy each, and launches one persistent kernel on the stream.
+// source descriptors.  A run copies the descriptors and the per-source tile
+// (and waveform chunk) prefix sums with one asynchronous copy and launches one
+// persistent kernel on the stream; the kernel resolves its (source, tile)
+// items from the prefix sums.
+//
+// A batch graph is a CUDA graph of that copy and those launches for a fixed
+// capacity of sources.  Its kernels read the number of sources' tiles from the
+// copied prefix sums, so one graph runs batches of any lengths and up to its
+// capacity of sources (the rest are empty descriptors); the per-source data
+// (buffers, lengths, sky position, start time, TDI set, waveform parameters)
+// are staging contents, not graph parameters.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -33,10 +41,26 @@ struct flr_batch_plan {
     unsigned char *d_stage;    // per-run descriptors, work items, waveform parameters
     size_t cap_device;
     int sms;
-    unsigned char *h_stage;    // pinned staging for descriptors and work items
+    unsigned char *h_stage;    // pinned staging for descriptors and prefix sums
     size_t cap_stage;
     cudaEvent_t stage_free;    // recorded after the staging copies of the last run
     bool stage_pending;
+    cudaEvent_t done;          // recorded after the kernels of the last run
+    bool done_pending;
+};
+
+struct flr_batch_graph {
+    flr_batch_plan *plan;
+    int cap;                   // sources per launch at most
+    bool waveforms, diag;
+    int chan;
+    unsigned char *h_stage[2];  // pinned staging, alternated between launches
+    unsigned char *d_stage;
+    cudaGraphExec_t exec[2];    // exec[b] copies from h_stage[b]
+    cudaEvent_t done[2];        // recorded after the launch that used buffer b
+    bool pending[2];
+    int next;                   // buffer of the next launch
+    int last;                   // buffer of the last launch (-1: none yet)
 };
 
 namespace {
@@ -47,6 +71,7 @@ int fail(int code, const std::string &msg) {
 }
 
 int cuda_fail(cudaError_t err, const std::string &what) {
+    cudaGetLastError();  // a handled error must not resurface in a later check
     return fail(FLR_E_CUDA, what + ": " + cudaGetErrorString(err));
 }
 
@@ -73,7 +98,126 @@ void release(flr_batch_plan *p) {
     if (p->d_stage) cudaFree(p->d_stage);
     if (p->h_stage) cudaFreeHost(p->h_stage);
     if (p->stage_free) cudaEventDestroy(p->stage_free);
+    if (p->done) cudaEventDestroy(p->done);
     delete p;
+}
+
+// Staging layout: descriptors | tile prefix sums | waveform parameters |
+// chunk prefix sums, each part 256-byte aligned.
+struct StageLayout {
+    size_t tiles, gb, chunks, bytes;
+};
+
+StageLayout stage_layout(int cap, bool waveforms) {
+    auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+    StageLayout l;
+    l.tiles = up(sizeof(flr::FusedSource) * (size_t)cap);
+    l.gb = up(l.tiles + sizeof(long) * ((size_t)cap + 1));
+    l.chunks = up(l.gb + (waveforms ? sizeof(flr::GbParams) * (size_t)cap : 0));
+    l.bytes = l.chunks + (waveforms ? sizeof(long) * ((size_t)cap + 1) : 0);
+    return l;
+}
+
+// Check the sources and write their staging image for `cap` descriptors
+// (entries num_sources..cap-1 are empty: no tiles, no chunks).  `diag` is set
+// when a source asks for diagnostics.
+int fill_stage(const flr_batch_plan *plan, const flr_batch_source *sources, int num_sources,
+               const flr_gb_params *gb, int cap, const StageLayout &lay, unsigned char *hs,
+               bool *diag) {
+    const int tile = plan->base.tile;
+    flr::FusedSource *srcs = reinterpret_cast<flr::FusedSource *>(hs);
+    long *tile_start = reinterpret_cast<long *>(hs + lay.tiles);
+    long *chunk_start = reinterpret_cast<long *>(hs + lay.chunks);
+    long tiles = 0, chunks = 0;
+    *diag = false;
+    for (int i = 0; i < num_sources; ++i) {
+        const flr_batch_source &s = sources[i];
+        if (!s.h || !s.out || s.n < 2 || s.projections_start < 0 ||
+            s.tdi_start < s.projections_start || 2LL * s.tdi_start >= s.n ||
+            s.n > (1LL << 31) - 1 || s.tdi_set < 0 || s.tdi_set >= plan->num_sets)
+            return fail(FLR_E_INVALID_ARGUMENT,
+                        "source " + std::to_string(i) +
+                            ": need h, out, 0 <= projections_start <= tdi_start < n/2, "
+                            "n < 2^31 and a valid tdi_set");
+        if (reinterpret_cast<uintptr_t>(s.h) % 16 != 0)
+            return fail(FLR_E_INVALID_ARGUMENT, "source " + std::to_string(i) +
+                                                    ": h (complex128) must be 16-byte aligned");
+        if ((s.d_rec_out == nullptr) != (s.d_em_out == nullptr))
+            return fail(FLR_E_INVALID_ARGUMENT, "d_rec_out and d_em_out go together");
+        flr::FusedSource d{};
+        d.h = static_cast<const double2 *>(s.h);
+        d.out = s.out;
+        d.n = (long)s.n;
+        d.ps = s.projections_start;
+        d.ts = s.tdi_start;
+        d.t0 = s.t0;
+        for (int c = 0; c < 3; ++c) {
+            d.k[c] = s.k[c];
+            d.u[c] = s.u[c];
+            d.v[c] = s.v[c];
+        }
+        d.tdi_set = s.tdi_set;
+        d.y_out = s.y_out;
+        d.d_rec_out = s.d_rec_out;
+        d.d_em_out = s.d_em_out;
+        d.d_tdi_out = s.d_tdi_out;
+        *diag = *diag || s.y_out || s.d_rec_out || s.d_tdi_out;
+        std::memcpy(srcs + i, &d, sizeof(d));
+        tile_start[i] = tiles;
+        tiles += (long)((s.n - 2LL * s.tdi_start + tile - 1) / tile);
+        if (gb) {
+            chunk_start[i] = chunks;
+            chunks += flr::gb_waveform_chunks((long)s.n);
+            flr::GbParams g{gb[i].A, gb[i].f, gb[i].fdot, gb[i].iota, gb[i].phi0, gb[i].psi};
+            std::memcpy(reinterpret_cast<flr::GbParams *>(hs + lay.gb) + i, &g, sizeof(g));
+        }
+    }
+    if (tiles > 0x7fffffffL) return fail(FLR_E_INVALID_ARGUMENT, "too many tiles");
+    if (cap > num_sources) {
+        std::memset(srcs + num_sources, 0, sizeof(flr::FusedSource) * (size_t)(cap - num_sources));
+        if (gb)
+            std::memset(reinterpret_cast<flr::GbParams *>(hs + lay.gb) + num_sources, 0,
+                        sizeof(flr::GbParams) * (size_t)(cap - num_sources));
+    }
+    for (int i = num_sources; i <= cap; ++i) {
+        tile_start[i] = tiles;
+        if (gb) chunk_start[i] = chunks;
+    }
+    return FLR_OK;
+}
+
+// The copy of a staging image to `d_stage` and the kernels that read it.
+cudaError_t enqueue(const flr_batch_plan *plan, const unsigned char *h_stage,
+                    unsigned char *d_stage, const StageLayout &lay, int cap, bool waveforms,
+                    bool diag, int chan, cudaEvent_t copied, cudaStream_t st) {
+    cudaError_t err = cudaMemcpyAsync(d_stage, h_stage, lay.bytes, cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess && copied) err = cudaEventRecord(copied, st);
+    if (err != cudaSuccess) return err;
+    const flr::FusedSource *d_src = reinterpret_cast<const flr::FusedSource *>(d_stage);
+    if (waveforms) {
+        err = flr::launch_gb_waveforms(
+            d_src, reinterpret_cast<const flr::GbParams *>(d_stage + lay.gb),
+            reinterpret_cast<const long *>(d_stage + lay.chunks), cap, plan->base.dt,
+            plan->sms * 8, st);
+        if (err != cudaSuccess) return err;
+    }
+    flr::FusedArgs a = plan->base;
+    a.sources = d_src;
+    a.tile_start = reinterpret_cast<const long *>(d_stage + lay.tiles);
+    a.num_sources = cap;
+    a.chan = chan;
+    return flr::launch_fused(plan->mixed, diag, a, plan->grid_max, plan->smem, st);
+}
+
+void release_graph(flr_batch_graph *g) {
+    if (!g) return;
+    for (int b = 0; b < 2; ++b) {
+        if (g->exec[b]) cudaGraphExecDestroy(g->exec[b]);
+        if (g->h_stage[b]) cudaFreeHost(g->h_stage[b]);
+        if (g->done[b]) cudaEventDestroy(g->done[b]);
+    }
+    if (g->d_stage) cudaFree(g->d_stage);
+    delete g;
 }
 
 }  // namespace
@@ -241,6 +385,18 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
         err = cudaMemcpy(static_cast<char *>(p->d_tables) + set_off, hsets.data(),
                          sizeof(flr::FusedTdiSet) * num_sets, cudaMemcpyHostToDevice);
     if (err == cudaSuccess) err = cudaEventCreateWithFlags(&p->stage_free, cudaEventDisableTiming);
+    if (err == cudaSuccess) err = cudaEventCreateWithFlags(&p->done, cudaEventDisableTiming);
+    int smem_optin = 0;
+    if (err == cudaSuccess)
+        err = cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                                     p->device);
+    if (err == cudaSuccess && p->smem > (size_t)smem_optin) {
+        release(p);
+        return fail(FLR_E_UNSUPPORTED, "tile " + std::to_string(tile) + " needs " +
+                                           std::to_string(p->smem) +
+                                           " B of shared memory per block; the device allows " +
+                                           std::to_string(smem_optin));
+    }
     int per_sm = 0;
     if (err == cudaSuccess) err = flr::fused_configure(p->mixed, p->smem, &per_sm);
     int sms = 0;
@@ -280,6 +436,7 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
 int flr_batch_plan_destroy(flr_batch_plan *plan) {
     if (!plan) return FLR_OK;
     if (plan->stage_pending) cudaEventSynchronize(plan->stage_free);
+    if (plan->done_pending) cudaEventSynchronize(plan->done);
     release(plan);
     return FLR_OK;
 }
@@ -303,51 +460,7 @@ static int batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int 
         return fail(FLR_E_INVALID_ARGUMENT, "invalid source list");
     if (chan != FLR_CHAN_XYZ && chan != FLR_CHAN_AET && chan != FLR_CHAN_AE)
         return fail(FLR_E_INVALID_ARGUMENT, "chan must be FLR_CHAN_XYZ, _AET or _AE");
-    const int tile = plan->base.tile;
-    std::vector<flr::FusedSource> srcs(num_sources);
-    size_t num_work = 0;
-    long num_chunks = 0;
-    std::vector<long> chunk_start(num_sources);
-    bool diag = false;
-    for (int i = 0; i < num_sources; ++i) {
-        const flr_batch_source &s = sources[i];
-        if (!s.h || !s.out || s.n < 2 || s.projections_start < 0 ||
-            s.tdi_start < s.projections_start || 2LL * s.tdi_start >= s.n ||
-            s.n > (1LL << 31) - 1 || s.tdi_set < 0 || s.tdi_set >= plan->num_sets)
-            return fail(FLR_E_INVALID_ARGUMENT,
-                        "source " + std::to_string(i) +
-                            ": need h, out, 0 <= projections_start <= tdi_start < n/2, "
-                            "n < 2^31 and a valid tdi_set");
-        if (reinterpret_cast<uintptr_t>(s.h) % 16 != 0)
-            return fail(FLR_E_INVALID_ARGUMENT, "source " + std::to_string(i) +
-                                                    ": h (complex128) must be 16-byte aligned");
-        flr::FusedSource &d = srcs[i];
-        d.h = static_cast<const double2 *>(s.h);
-        d.out = s.out;
-        d.n = (long)s.n;
-        d.ps = s.projections_start;
-        d.ts = s.tdi_start;
-        d.t0 = s.t0;
-        for (int c = 0; c < 3; ++c) {
-            d.k[c] = s.k[c];
-            d.u[c] = s.u[c];
-            d.v[c] = s.v[c];
-        }
-        d.tdi_set = s.tdi_set;
-        d.pad = 0;
-        d.y_out = s.y_out;
-        d.d_rec_out = s.d_rec_out;
-        d.d_em_out = s.d_em_out;
-        d.d_tdi_out = s.d_tdi_out;
-        diag = diag || s.y_out || s.d_rec_out || s.d_tdi_out;
-        if ((s.d_rec_out == nullptr) != (s.d_em_out == nullptr))
-            return fail(FLR_E_INVALID_ARGUMENT, "d_rec_out and d_em_out go together");
-        num_work += (size_t)((s.n - 2LL * s.tdi_start + tile - 1) / tile);
-        chunk_start[i] = num_chunks;
-        num_chunks += flr::gb_waveform_chunks((long)s.n);
-    }
-    if (num_work == 0) return FLR_OK;
-    if (num_work > (size_t)0x7fffffff) return fail(FLR_E_INVALID_ARGUMENT, "too many tiles");
+    if (num_sources == 0) return FLR_OK;
 
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t err = cudaSuccess;
@@ -357,65 +470,43 @@ static int batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int 
         if (err != cudaSuccess) return cuda_fail(err, "waiting for the previous run's copies");
         plan->stage_pending = false;
     }
-    // staging layout: sources | work items | gb params | chunk starts
-    auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
-    const size_t src_bytes = sizeof(flr::FusedSource) * srcs.size();
-    const size_t work_off = up(src_bytes);
-    const size_t gb_off = up(work_off + sizeof(int2) * num_work);
-    const size_t gb_bytes = gb ? sizeof(flr::GbParams) * srcs.size() : 0;
-    const size_t cs_off = up(gb_off + gb_bytes);
-    const size_t stage_bytes = cs_off + (gb ? sizeof(long) * srcs.size() : 0);
-    if (stage_bytes > plan->cap_stage) {
+    const StageLayout lay = stage_layout(num_sources, gb != nullptr);
+    if (lay.bytes > plan->cap_stage) {
         if (plan->h_stage) cudaFreeHost(plan->h_stage);
         plan->h_stage = nullptr;
         plan->cap_stage = 0;
-        err = cudaMallocHost(&plan->h_stage, stage_bytes * 2);
+        err = cudaMallocHost(&plan->h_stage, lay.bytes * 2);
         if (err != cudaSuccess) return cuda_fail(err, "allocating the staging buffer");
-        plan->cap_stage = stage_bytes * 2;
+        plan->cap_stage = lay.bytes * 2;
     }
-    if (stage_bytes > plan->cap_device) {
-        if (plan->d_stage) cudaFree(plan->d_stage);
+    bool diag = false;
+    rc = fill_stage(plan, sources, num_sources, gb, num_sources, lay, plan->h_stage, &diag);
+    if (rc) return rc;
+    // the device staging buffer is reused: a previous run on another stream
+    // must have finished reading it
+    if (plan->done_pending) {
+        err = cudaStreamWaitEvent(st, plan->done, 0);
+        if (err != cudaSuccess) return cuda_fail(err, "ordering after the previous run");
+    }
+    if (lay.bytes > plan->cap_device) {
+        if (plan->d_stage) {
+            err = cudaStreamSynchronize(st);
+            if (err == cudaSuccess) err = cudaFree(plan->d_stage);
+            if (err != cudaSuccess) return cuda_fail(err, "releasing the staging buffer");
+        }
         plan->d_stage = nullptr;
         plan->cap_device = 0;
-        err = cudaMalloc(&plan->d_stage, stage_bytes * 2);
-        if (err != cudaSuccess) return cuda_fail(err, "allocating the work list");
-        plan->cap_device = stage_bytes * 2;
+        err = cudaMalloc(&plan->d_stage, lay.bytes * 2);
+        if (err != cudaSuccess) return cuda_fail(err, "allocating the staging buffer");
+        plan->cap_device = lay.bytes * 2;
     }
-    unsigned char *hs = plan->h_stage;
-    std::memcpy(hs, srcs.data(), src_bytes);
-    int2 *work = reinterpret_cast<int2 *>(hs + work_off);
-    size_t w = 0;
-    for (int i = 0; i < num_sources; ++i) {
-        const long tiles = (long)((sources[i].n - 2LL * sources[i].tdi_start + tile - 1) / tile);
-        for (long t = 0; t < tiles; ++t) work[w++] = make_int2(i, (int)t);
-    }
-    if (gb) {
-        flr::GbParams *gp = reinterpret_cast<flr::GbParams *>(hs + gb_off);
-        for (int i = 0; i < num_sources; ++i)
-            gp[i] = flr::GbParams{gb[i].A, gb[i].f, gb[i].fdot, gb[i].iota, gb[i].phi0, gb[i].psi};
-        std::memcpy(hs + cs_off, chunk_start.data(), sizeof(long) * srcs.size());
-    }
-    err = cudaMemcpyAsync(plan->d_stage, hs, stage_bytes, cudaMemcpyHostToDevice, st);
-    if (err == cudaSuccess) err = cudaEventRecord(plan->stage_free, st);
-    if (err != cudaSuccess) return cuda_fail(err, "copying the work list");
+    err = enqueue(plan, plan->h_stage, plan->d_stage, lay, num_sources, gb != nullptr, diag, chan,
+                  plan->stage_free, st);
     plan->stage_pending = true;
-
-    const flr::FusedSource *d_src = reinterpret_cast<const flr::FusedSource *>(plan->d_stage);
-    if (gb) {
-        err = flr::launch_gb_waveforms(
-            d_src, reinterpret_cast<const flr::GbParams *>(plan->d_stage + gb_off),
-            reinterpret_cast<const long *>(plan->d_stage + cs_off), num_sources, num_chunks,
-            plan->base.dt, plan->sms * 8, st);
-        if (err != cudaSuccess) return cuda_fail(err, "launching the waveform kernel");
-    }
-    flr::FusedArgs a = plan->base;
-    a.sources = d_src;
-    a.work = reinterpret_cast<const int2 *>(plan->d_stage + work_off);
-    a.num_work = (int)num_work;
-    a.chan = chan;
-    const int grid = (int)std::min<size_t>(num_work, (size_t)plan->grid_max);
-    err = flr::launch_fused(plan->mixed, diag, a, grid, plan->smem, st);
-    if (err != cudaSuccess) return cuda_fail(err, "launching the fused kernel");
+    if (err != cudaSuccess) return cuda_fail(err, "launching the batch");
+    err = cudaEventRecord(plan->done, st);
+    if (err != cudaSuccess) return cuda_fail(err, "recording the batch");
+    plan->done_pending = true;
     return FLR_OK;
 }
 
@@ -429,6 +520,105 @@ int flr_batch_run_gb(flr_batch_plan *plan, const flr_batch_source *sources,
     if (num_sources > 0 && !params)
         return fail(FLR_E_INVALID_ARGUMENT, "params must not be NULL");
     return batch_run(plan, sources, num_sources, params, chan, stream);
+}
+
+int flr_batch_graph_create(flr_batch_plan *plan, int max_sources, int flags, int chan,
+                           flr_batch_graph **out) {
+    flr::set_last_error("");
+    if (!out) return fail(FLR_E_INVALID_ARGUMENT, "out must not be NULL");
+    *out = nullptr;
+    if (!plan) return fail(FLR_E_INVALID_ARGUMENT, "plan must not be NULL");
+    int rc = current_device_is(plan->device);
+    if (rc) return rc;
+    if (max_sources < 1 || max_sources > (1 << 20))
+        return fail(FLR_E_INVALID_ARGUMENT, "max_sources must be in [1, 2^20]");
+    if (flags & ~(FLR_GRAPH_WAVEFORMS | FLR_GRAPH_DIAGNOSTICS))
+        return fail(FLR_E_INVALID_ARGUMENT, "unknown graph flags");
+    if (chan != FLR_CHAN_XYZ && chan != FLR_CHAN_AET && chan != FLR_CHAN_AE)
+        return fail(FLR_E_INVALID_ARGUMENT, "chan must be FLR_CHAN_XYZ, _AET or _AE");
+    flr_batch_graph *g = new flr_batch_graph();
+    g->plan = plan;
+    g->cap = max_sources;
+    g->waveforms = (flags & FLR_GRAPH_WAVEFORMS) != 0;
+    g->diag = (flags & FLR_GRAPH_DIAGNOSTICS) != 0;
+    g->chan = chan;
+    g->last = -1;
+    const StageLayout lay = stage_layout(g->cap, g->waveforms);
+    cudaError_t err = cudaMalloc(&g->d_stage, lay.bytes);
+    for (int b = 0; b < 2 && err == cudaSuccess; ++b) {
+        err = cudaMallocHost(&g->h_stage[b], lay.bytes);
+        if (err == cudaSuccess) std::memset(g->h_stage[b], 0, lay.bytes);
+        if (err == cudaSuccess) err = cudaEventCreateWithFlags(&g->done[b], cudaEventDisableTiming);
+    }
+    cudaStream_t cs = nullptr;
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    for (int b = 0; b < 2 && err == cudaSuccess; ++b) {
+        err = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (err != cudaSuccess) break;
+        const cudaError_t e_enq = enqueue(plan, g->h_stage[b], g->d_stage, lay, g->cap,
+                                          g->waveforms, g->diag, chan, nullptr, cs);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e_end = cudaStreamEndCapture(cs, &graph);
+        err = (e_enq != cudaSuccess) ? e_enq : e_end;
+        if (err == cudaSuccess) err = cudaGraphInstantiate(&g->exec[b], graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+    }
+    if (cs) cudaStreamDestroy(cs);
+    if (err != cudaSuccess) {
+        release_graph(g);
+        return cuda_fail(err, "capturing the batch graph");
+    }
+    *out = g;
+    return FLR_OK;
+}
+
+int flr_batch_graph_launch(flr_batch_graph *g, const flr_batch_source *sources,
+                           const flr_gb_params *params, int num_sources, void *stream) {
+    flr::set_last_error("");
+    if (!g) return fail(FLR_E_INVALID_ARGUMENT, "graph must not be NULL");
+    int rc = current_device_is(g->plan->device);
+    if (rc) return rc;
+    if (num_sources < 0 || num_sources > g->cap || (num_sources > 0 && !sources))
+        return fail(FLR_E_INVALID_ARGUMENT, "need 0.." + std::to_string(g->cap) + " sources");
+    if (g->waveforms && num_sources > 0 && !params)
+        return fail(FLR_E_INVALID_ARGUMENT, "this graph generates waveforms: params required");
+    if (!g->waveforms && params)
+        return fail(FLR_E_INVALID_ARGUMENT, "this graph has no waveform stage");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t err = cudaSuccess;
+    const int b = g->next;
+    if (g->pending[b]) {  // the launch that last used this staging buffer
+        err = cudaEventSynchronize(g->done[b]);
+        if (err != cudaSuccess) return cuda_fail(err, "waiting for an earlier launch");
+        g->pending[b] = false;
+    }
+    const StageLayout lay = stage_layout(g->cap, g->waveforms);
+    bool diag = false;
+    rc = fill_stage(g->plan, sources, num_sources, g->waveforms ? params : nullptr, g->cap, lay,
+                    g->h_stage[b], &diag);
+    if (rc) return rc;
+    if (diag && !g->diag)
+        return fail(FLR_E_INVALID_ARGUMENT,
+                    "diagnostics need a graph created with FLR_GRAPH_DIAGNOSTICS");
+    if (g->last >= 0 && g->pending[g->last]) {  // the device staging buffer is shared
+        err = cudaStreamWaitEvent(st, g->done[g->last], 0);
+        if (err != cudaSuccess) return cuda_fail(err, "ordering after the previous launch");
+    }
+    err = cudaGraphLaunch(g->exec[b], st);
+    if (err == cudaSuccess) err = cudaEventRecord(g->done[b], st);
+    if (err != cudaSuccess) return cuda_fail(err, "launching the batch graph");
+    g->pending[b] = true;
+    g->last = b;
+    g->next = 1 - b;
+    return FLR_OK;
+}
+
+int flr_batch_graph_destroy(flr_batch_graph *g) {
+    if (!g) return FLR_OK;
+    for (int b = 0; b < 2; ++b)
+        if (g->pending[b]) cudaEventSynchronize(g->done[b]);
+    release_graph(g);
+    return FLR_OK;
 }
 
 }  // extern "C"

@@ -21,6 +21,7 @@ int fail(int code, const std::string &msg) {
 }
 
 int cuda_fail(cudaError_t err, const char *what) {
+    cudaGetLastError();  // a handled error must not resurface in a later check
     return fail(FLR_E_CUDA, std::string(what) + ": " + cudaGetErrorString(err));
 }
 

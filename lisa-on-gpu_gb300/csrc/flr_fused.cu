@@ -1,5 +1,6 @@
-// Batched, fused response + TDI (sm_103a): one persistent launch over a
-// flattened (source, tile) work list.
+// Batched, fused response + TDI (sm_103a): one persistent launch over the
+// flattened (source, tile) items of a batch, resolved on the device from
+// per-source tile prefix sums (no work list is uploaded).
 //
 // A work item is T consecutive output samples [o0, o1) of one source.  The CTA
 //   1. finds the input window its link streams need (geometry at the two ends
@@ -382,9 +383,21 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
 
     uint32_t phase = 0;
     int loaded_set = -1;
-    for (int wi = blockIdx.x; wi < a.num_work; wi += gridDim.x) {
-        const int2 item = a.work[wi];
-        const FusedSource &src = a.sources[item.x];
+    const long num_work = __ldg(a.tile_start + a.num_sources);
+    int si = 0;
+    for (long wi = blockIdx.x; wi < num_work; wi += gridDim.x) {
+        // source of item wi: the last s with tile_start[s] <= wi (a block's
+        // items only grow, so the search starts at its previous source)
+        int hi = a.num_sources - 1;
+        while (si < hi) {
+            const int mid = (si + hi + 1) >> 1;
+            if (__ldg(a.tile_start + mid) <= wi)
+                si = mid;
+            else
+                hi = mid - 1;
+        }
+        const long tile_idx = wi - __ldg(a.tile_start + si);
+        const FusedSource &src = a.sources[si];
         const long n = src.n;
         const int ps = src.ps, ts = src.ts;
         const double t0 = src.t0;
@@ -409,8 +422,18 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
             loaded_set = src.tdi_set;
         }
 
-        const long o0 = ts + (long)item.y * a.tile;
+        const long o0 = ts + tile_idx * a.tile;
         const long o1 = min(o0 + (long)a.tile, n - ts);
+        // the first and last tiles also write the zeros of the edge zones
+        // [0, ts) and [n - ts, n), so outputs need no clearing beforehand
+        if (tile_idx == 0 || o1 == n - ts) {
+            const long e0 = (tile_idx == 0) ? 0 : n - ts;
+            for (int c = 0; c < 3; ++c)
+                for (long i = e0 + tid; i < e0 + ts; i += kThreads) src.out[c * n + i] = 0.0;
+            if (tile_idx == 0 && o1 == n - ts)
+                for (int c = 0; c < 3; ++c)
+                    for (long i = n - ts + tid; i < n; i += kThreads) src.out[c * n + i] = 0.0;
+        }
         const long ya = max(o0 - a.y_halo, 0L);
         const long yb = min(o1 + a.y_halo, n);
         const long yfirst = max(ya, (long)ps), ylast = min(yb, n - ps);  // y computed here
@@ -680,7 +703,7 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
                 // lisaanalysistools AET: (Z-X)/sqrt2, (X-2Y+Z)/sqrt6, (X+Y+Z)/sqrt3
                 out[i] = (Z - X) / 1.4142135623730951;
                 out[n + i] = (X - 2.0 * Yc + Z) / 2.449489742783178;
-                if (a.chan == kChanAET) out[2 * n + i] = (X + Yc + Z) / 1.7320508075688772;
+                out[2 * n + i] = (a.chan == kChanAET) ? (X + Yc + Z) / 1.7320508075688772 : 0.0;
             }
         }
         __syncthreads();
@@ -714,7 +737,7 @@ cudaError_t fused_configure(bool mixed, size_t smem_bytes, int *blocks_per_sm) {
 
 cudaError_t launch_fused(bool mixed, bool diag, const FusedArgs &a, int grid, size_t smem_bytes,
                          cudaStream_t stream) {
-    if (a.num_work <= 0) return cudaSuccess;
+    if (a.num_sources <= 0) return cudaSuccess;
     void *args[] = {const_cast<FusedArgs *>(&a)};
     return cudaLaunchKernel(fused_fn(mixed, diag), dim3(grid), dim3(kThreads), args, smem_bytes,
                             stream);

@@ -57,8 +57,12 @@ struct FusedArgs {
     OrbitTables orb;
     LagrangeTables lt;
     const FusedSource *sources;
-    const int2 *work;          // (source, tile) items
-    int num_work;
+    // tile_start[s] = tiles of sources 0..s-1; tile_start[num_sources] = all
+    // tiles of the run.  Work item w is tile w - tile_start[s] of the source s
+    // with tile_start[s] <= w < tile_start[s + 1].  The total is read on the
+    // device, so a captured launch can run batches of any lengths.
+    const long *tile_start;
+    int num_sources;
     const FusedTdiSet *sets;
     int num_sets;
     const float4 *a_tab;       // per A-table knot: (A hi, A lo, dA hi, dA lo), dA = A[k+1]-A[k]
@@ -79,9 +83,11 @@ struct GbParams {
 };
 
 long gb_waveform_chunks(long n);
+// chunk_start[s] = waveform chunks of sources 0..s-1 (num_sources + 1 entries;
+// the last is the total, read on the device).
 cudaError_t launch_gb_waveforms(const FusedSource *src, const GbParams *par,
-                                const long *chunk_start, int num_sources, long num_chunks,
-                                double dt, int grid, cudaStream_t stream);
+                                const long *chunk_start, int num_sources, double dt, int grid,
+                                cudaStream_t stream);
 
 size_t fused_smem_bytes(bool mixed, int win_max, int y_max);
 cudaError_t fused_configure(bool mixed, size_t smem_bytes, int *blocks_per_sm);

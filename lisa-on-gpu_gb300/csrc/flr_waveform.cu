@@ -10,7 +10,8 @@
 // sincos, so it agrees with the host generator to a few ulp.
 //
 // One persistent launch covers every source of a batch: work items are
-// (source, chunk of kChunk samples), strided over the grid.
+// (source, chunk of kChunk samples), strided over the grid; the source of a
+// chunk is found by binary search in the per-source chunk prefix sums.
 #include <cuda_runtime.h>
 
 #include "flr_fused.h"
@@ -23,7 +24,8 @@ constexpr int kChunk = 2048;
 
 __global__ void __launch_bounds__(kThreads)
 gb_waveform_kernel(const FusedSource *src, const GbParams *par, const long *chunk_start,
-                   int num_sources, long num_chunks, double dt) {
+                   int num_sources, double dt) {
+    const long num_chunks = chunk_start[num_sources];
     for (long c = blockIdx.x; c < num_chunks; c += gridDim.x) {
         // source of chunk c: chunk_start is the exclusive prefix sum of chunks
         int lo = 0, hi = num_sources - 1;
@@ -60,11 +62,10 @@ gb_waveform_kernel(const FusedSource *src, const GbParams *par, const long *chun
 long gb_waveform_chunks(long n) { return (n + kChunk - 1) / kChunk; }
 
 cudaError_t launch_gb_waveforms(const FusedSource *src, const GbParams *par,
-                                const long *chunk_start, int num_sources, long num_chunks,
-                                double dt, int grid, cudaStream_t stream) {
-    if (num_chunks <= 0) return cudaSuccess;
-    gb_waveform_kernel<<<grid, kThreads, 0, stream>>>(src, par, chunk_start, num_sources,
-                                                      num_chunks, dt);
+                                const long *chunk_start, int num_sources, double dt, int grid,
+                                cudaStream_t stream) {
+    if (num_sources <= 0) return cudaSuccess;
+    gb_waveform_kernel<<<grid, kThreads, 0, stream>>>(src, par, chunk_start, num_sources, dt);
     return cudaGetLastError();
 }
 

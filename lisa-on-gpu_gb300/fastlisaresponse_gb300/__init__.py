@@ -8,7 +8,8 @@ C ABI in ``include/flr_gb300.h``) through ctypes.  There is no CPU backend.
 
 from ._build import build, needs_build
 from ._lib import FLRError, describe_status, library_path
-from .batch import BatchedResponseTDI
+from . import autotune
+from .batch import BatchedResponseTDI, BatchGraph
 from .binding import LISAResponseWrap, LISAResponseWrapGPU, OrbitsWrap, OrbitsWrapGPU_responselisa
 from .orbits import EqualArmlengthOrbits, KeplerianOrbits, Orbits
 from .serve import Request, ResponseServer
@@ -20,9 +21,9 @@ from .waveforms import GBWave, gb_waveform, time_grid
 __version__ = "0.1.0"
 
 __all__ = [
-    "AET", "BatchedResponseTDI", "EqualArmlengthOrbits", "FLRError", "GBWave", "KeplerianOrbits",
+    "AET", "BatchGraph", "BatchedResponseTDI", "EqualArmlengthOrbits", "FLRError", "GBWave", "KeplerianOrbits",
     "LISAResponseWrap", "LISAResponseWrapGPU", "Orbits", "OrbitsWrap",
-    "OrbitsWrapGPU_responselisa", "ResponseWrapper", "build", "describe_status",
+    "OrbitsWrapGPU_responselisa", "ResponseWrapper", "autotune", "build", "describe_status",
     "gb_waveform", "get_overlap", "lagrange_tables", "library_path", "needs_build",
     "pyResponseTDI", "Request", "ResponseServer", "sky_basis", "tdi_unit_tables", "time_grid",
 ]

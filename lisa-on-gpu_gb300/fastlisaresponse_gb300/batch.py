@@ -101,7 +101,20 @@ def _plan_fns():
     lib.flr_batch_run_gb.argtypes = [p, ctypes.POINTER(_Source), ctypes.POINTER(_GbParams), i, i,
                                      p]
     lib.flr_batch_run_gb.restype = i
+    lib.flr_batch_graph_create.argtypes = [p, i, i, i, ctypes.POINTER(p)]
+    lib.flr_batch_graph_create.restype = i
+    lib.flr_batch_graph_launch.argtypes = [p, ctypes.POINTER(_Source), ctypes.POINTER(_GbParams),
+                                           i, p]
+    lib.flr_batch_graph_launch.restype = i
+    lib.flr_batch_graph_destroy.argtypes = [p]
+    lib.flr_batch_graph_destroy.restype = i
     return lib
+
+
+SOURCE_DTYPE = np.dtype(_Source)
+GB_DTYPE = np.dtype(_GbParams)
+GRAPH_WAVEFORMS = 0x1
+GRAPH_DIAGNOSTICS = 0x2
 
 
 class BatchedResponseTDI:
@@ -116,12 +129,17 @@ class BatchedResponseTDI:
         tdi_chan: "XYZ", "AET" or "AE".
         precision: "fp64" (bit-identical to the plain path) or "mixed".
         t_buffer: garbage time removed at each end [s] (as in get_projections).
-        tile: output samples per work item (0 = library default).
+        tile: output samples per work item (0 = library default, 512), or
+            "auto": the fastest of the autotuner's candidates for this
+            configuration, measured on first use and cached
+            (:mod:`fastlisaresponse_gb300.autotune`).
+        tune_lengths: source lengths of the batch the autotuner times
+            (default 32 x 2^18).
     """
 
     def __init__(self, sampling_frequency, order=25, tdi="1st generation",
                  orbits=EqualArmlengthOrbits, tdi_chan="XYZ", precision="fp64",
-                 t_buffer=10000.0, tile=0, force_backend=None):
+                 t_buffer=10000.0, tile=0, force_backend=None, tune_lengths=None):
         if precision not in PRECISION:
             raise ValueError("precision must be 'fp64' or 'mixed'")
         if tdi_chan not in CHANNELS:
@@ -165,6 +183,15 @@ class BatchedResponseTDI:
             self._keep.append(arrs)
             units[i] = _TdiUnits(tb["num_units"], *[a.ctypes.data for a in arrs],
                                  len(tb["tdi_link_combinations"]))
+        self.tune = None
+        if isinstance(tile, str):
+            if tile != "auto":
+                raise ValueError("tile must be an integer or 'auto'")
+            from .autotune import best_tile
+
+            self.tune = best_tile(sampling_frequency, order, tdi, orbits, precision, tdi_chan,
+                                  t_buffer, self.device, lengths=tune_lengths)
+            tile = self.tune["tile"]
         lib = _plan_fns()
         plan = ctypes.c_void_p()
         with torch.cuda.device(self.device):
@@ -174,6 +201,7 @@ class BatchedResponseTDI:
                                            int(tile), ctypes.byref(plan))
         _lib.check(rc)
         self._plan = plan
+        self._graphs = {}
         info = (ctypes.c_int * 7)()
         lib.flr_batch_plan_info(plan, info, 7)
         self.plan_info = dict(zip(("tile", "y_halo", "win_max", "y_max", "smem_bytes",
@@ -181,6 +209,8 @@ class BatchedResponseTDI:
 
     def __del__(self):
         try:
+            for g in getattr(self, "_graphs", {}).values():
+                g.close()
             if getattr(self, "_plan", None) is not None:
                 _lib.lib().flr_batch_plan_destroy(self._plan)
                 self._plan = None
@@ -188,7 +218,7 @@ class BatchedResponseTDI:
             pass
 
     def __call__(self, h: Sequence, lam, beta, t0=0.0, tdi_set=0, out: Optional[Sequence] = None,
-                 stream=None, diagnostics: bool = False):
+                 stream=None, diagnostics: bool = False, use_graph: bool = False):
         """Evaluate the batch.
 
         Args:
@@ -198,59 +228,26 @@ class BatchedResponseTDI:
                 broadcast).
             t0: start time per source (scalar broadcasts).
             tdi_set: TDI set index per source (scalar broadcasts).
-            out: optional list of (3, n) float64 CUDA tensors to write into
-                (zeroed by the caller); allocated (zeros) when omitted.
+            out: optional list of contiguous (3, n) float64 CUDA tensors to
+                write into (every sample is written); allocated when omitted.
             diagnostics: also return, per source, the link streams and the
                 integer delays the kernel used (for the output samples).
+            use_graph: run through the CUDA graph of this batch's size bucket
+                (captured on first use; see :meth:`graph`).
         Returns:
             list of (3, n) tensors: rows X, Y, Z (or A, E, T / A, E and a
             zero third row); samples within t_buffer of either end are zero.
             With diagnostics, (outs, diags) where diags[i] is a dict of
             "y" (6, n), "d_rec" / "d_em" (6, n) and "d_tdi" (units, n).
         """
-        ns = len(h)
-        lam = np.broadcast_to(np.asarray(lam, dtype=np.float64), (ns,))
-        beta = np.broadcast_to(np.asarray(beta, dtype=np.float64), (ns,))
-        t0 = np.broadcast_to(np.asarray(t0, dtype=np.float64), (ns,))
-        sets = np.broadcast_to(np.asarray(tdi_set, dtype=np.int64), (ns,))
         dev = self.device
         hs = [_as_device(x, dev, torch.complex128) for x in h]
-        outs = list(out) if out is not None else [
-            torch.zeros((3, len(x)), dtype=torch.float64, device=dev) for x in hs]
-        srcs = (_Source * ns)()
-        diags = []
-        for i in range(ns):
-            n = len(hs[i])
-            o = outs[i]
-            if tuple(o.shape) != (3, n) or o.dtype != torch.float64 or not o.is_contiguous():
-                raise ValueError(f"out[{i}] must be a contiguous (3, {n}) float64 tensor")
-            k, u, v = sky_basis(float(lam[i]), float(beta[i]))
-            ptrs = [None] * 4
-            if diagnostics:
-                nu = self.tdi_sets[int(sets[i])]["num_units"]
-                dg = {"y": torch.zeros((6, n), dtype=torch.float64, device=dev),
-                      "d_rec": torch.zeros((6, n), dtype=torch.int32, device=dev),
-                      "d_em": torch.zeros((6, n), dtype=torch.int32, device=dev),
-                      "d_tdi": torch.zeros((nu, n), dtype=torch.int32, device=dev)}
-                diags.append(dg)
-                ptrs = [dg["y"].data_ptr(), dg["d_rec"].data_ptr(), dg["d_em"].data_ptr(),
-                        dg["d_tdi"].data_ptr()]
-            srcs[i] = _Source(hs[i].data_ptr(), o.data_ptr(), n, self.projections_start_ind,
-                              self.tdi_start_ind, float(t0[i]), (ctypes.c_double * 3)(*k),
-                              (ctypes.c_double * 3)(*u), (ctypes.c_double * 3)(*v),
-                              int(sets[i]), 0, *ptrs)
-        if stream is None:
-            stream = torch.cuda.current_stream(dev)
-        lib = _plan_fns()
-        with torch.cuda.device(dev):
-            rc = lib.flr_batch_run(self._plan, srcs, ns, CHANNELS[self.tdi_chan],
-                                   ctypes.c_void_p(stream.cuda_stream))
-        _lib.check(rc)
-        self._last_inputs = hs  # keep the inputs alive until the next call
-        return (outs, diags) if diagnostics else outs
+        lengths = [len(x) for x in hs]
+        return self._run(hs, None, lengths, lam, beta, t0, tdi_set, out, stream, diagnostics,
+                         self._bucket(len(hs), False, diagnostics) if use_graph else None)
 
     def run_gb(self, params, lengths, lam, beta, t0=0.0, tdi_set=0, h=None, out=None,
-               stream=None):
+               stream=None, use_graph: bool = False):
         """Generate galactic-binary waveforms on the device and evaluate them.
 
         Args:
@@ -259,46 +256,167 @@ class BatchedResponseTDI:
             lam, beta, t0, tdi_set: as for __call__ (scalars broadcast).
             h: optional list of complex128 CUDA buffers of the given lengths
                 that receive the waveforms (allocated when omitted).
-            out: optional list of zeroed (3, n) float64 CUDA tensors.
+            out: optional list of (3, n) float64 CUDA tensors.
+            use_graph: as for __call__.
         Returns:
             (outs, hs): the TDI channels and the generated waveforms.
         """
         params = np.asarray(params, dtype=np.float64).reshape(-1, 6)
         ns = len(params)
-        lengths = np.broadcast_to(np.asarray(lengths, dtype=np.int64), (ns,))
+        lengths = [int(n) for n in np.broadcast_to(np.asarray(lengths, dtype=np.int64), (ns,))]
+        dev = self.device
+        hs = list(h) if h is not None else [
+            torch.empty(n, dtype=torch.complex128, device=dev) for n in lengths]
+        for i, n in enumerate(lengths):
+            if hs[i].numel() != n or hs[i].dtype != torch.complex128 or not hs[i].is_cuda:
+                raise ValueError(f"h[{i}] must be a complex128 CUDA buffer of {n} samples")
+        outs = self._run(hs, params, lengths, lam, beta, t0, tdi_set, out, stream, False,
+                         self._bucket(ns, True, False) if use_graph else None)
+        return outs, hs
+
+    # -- internals ----------------------------------------------------------------
+    def _run(self, hs, params, lengths, lam, beta, t0, tdi_set, out, stream, diagnostics, graph):
+        ns = len(hs)
+        dev = self.device
         lam = np.broadcast_to(np.asarray(lam, dtype=np.float64), (ns,))
         beta = np.broadcast_to(np.asarray(beta, dtype=np.float64), (ns,))
         t0 = np.broadcast_to(np.asarray(t0, dtype=np.float64), (ns,))
         sets = np.broadcast_to(np.asarray(tdi_set, dtype=np.int64), (ns,))
-        dev = self.device
-        hs = list(h) if h is not None else [
-            torch.empty(int(n), dtype=torch.complex128, device=dev) for n in lengths]
-        outs = list(out) if out is not None else [
-            torch.zeros((3, int(n)), dtype=torch.float64, device=dev) for n in lengths]
-        srcs = (_Source * ns)()
-        gbs = (_GbParams * ns)()
+        if out is not None:
+            outs = list(out)
+            if len(outs) != ns:
+                raise ValueError("need one output per source")
+            for i, o in enumerate(outs):
+                n = lengths[i]
+                if (tuple(o.shape) != (3, n) or o.dtype != torch.float64 or not o.is_cuda
+                        or not o.is_contiguous()):
+                    raise ValueError(f"out[{i}] must be a contiguous (3, {n}) float64 CUDA tensor")
+        else:
+            outs = [torch.empty((3, n), dtype=torch.float64, device=dev) for n in lengths]
+        srcs = np.zeros(ns, dtype=SOURCE_DTYPE)
+        srcs["h"] = [x.data_ptr() for x in hs]
+        srcs["out"] = [o.data_ptr() for o in outs]
+        srcs["n"] = lengths
+        srcs["projections_start"] = self.projections_start_ind
+        srcs["tdi_start"] = self.tdi_start_ind
+        srcs["t0"] = t0
+        srcs["tdi_set"] = sets
         for i in range(ns):
-            n = int(lengths[i])
-            if hs[i].numel() != n or hs[i].dtype != torch.complex128 or not hs[i].is_cuda:
-                raise ValueError(f"h[{i}] must be a complex128 CUDA buffer of {n} samples")
-            if tuple(outs[i].shape) != (3, n) or outs[i].dtype != torch.float64:
-                raise ValueError(f"out[{i}] must be a (3, {n}) float64 tensor")
-            k, u, v = sky_basis(float(lam[i]), float(beta[i]))
-            srcs[i] = _Source(hs[i].data_ptr(), outs[i].data_ptr(), n, self.projections_start_ind,
-                              self.tdi_start_ind, float(t0[i]), (ctypes.c_double * 3)(*k),
-                              (ctypes.c_double * 3)(*u), (ctypes.c_double * 3)(*v),
-                              int(sets[i]), 0)
-            gbs[i] = _GbParams(*[float(x) for x in params[i]])
+            srcs["k"][i], srcs["u"][i], srcs["v"][i] = sky_basis(float(lam[i]), float(beta[i]))
+        diags = []
+        if diagnostics:
+            for i in range(ns):
+                n, nu = lengths[i], self.tdi_sets[int(sets[i])]["num_units"]
+                dg = {"y": torch.zeros((6, n), dtype=torch.float64, device=dev),
+                      "d_rec": torch.zeros((6, n), dtype=torch.int32, device=dev),
+                      "d_em": torch.zeros((6, n), dtype=torch.int32, device=dev),
+                      "d_tdi": torch.zeros((nu, n), dtype=torch.int32, device=dev)}
+                diags.append(dg)
+                srcs["y_out"][i] = dg["y"].data_ptr()
+                srcs["d_rec_out"][i] = dg["d_rec"].data_ptr()
+                srcs["d_em_out"][i] = dg["d_em"].data_ptr()
+                srcs["d_tdi_out"][i] = dg["d_tdi"].data_ptr()
+        gbs = None
+        if params is not None:
+            gbs = np.ascontiguousarray(params, dtype=np.float64).view(GB_DTYPE).reshape(ns)
         if stream is None:
             stream = torch.cuda.current_stream(dev)
         lib = _plan_fns()
+        src_p = srcs.ctypes.data_as(ctypes.POINTER(_Source))
+        gb_p = gbs.ctypes.data_as(ctypes.POINTER(_GbParams)) if gbs is not None else None
+        st = ctypes.c_void_p(stream.cuda_stream)
         with torch.cuda.device(dev):
-            rc = lib.flr_batch_run_gb(self._plan, srcs, gbs, ns, CHANNELS[self.tdi_chan],
-                                      ctypes.c_void_p(stream.cuda_stream))
+            if graph is not None:
+                rc = lib.flr_batch_graph_launch(graph._graph, src_p, gb_p, ns, st)
+            elif gbs is not None:
+                rc = lib.flr_batch_run_gb(self._plan, src_p, gb_p, ns, CHANNELS[self.tdi_chan], st)
+            else:
+                rc = lib.flr_batch_run(self._plan, src_p, ns, CHANNELS[self.tdi_chan], st)
         _lib.check(rc)
-        return outs, hs
+        self._last_inputs = hs  # keep the inputs alive until the next call
+        return (outs, diags) if diagnostics else outs
+
+    def _bucket(self, ns: int, waveforms: bool, diagnostics: bool) -> "BatchGraph":
+        cap = max(8, 1 << max(0, int(ns) - 1).bit_length())
+        key = (cap, waveforms, diagnostics)
+        g = self._graphs.get(key)
+        if g is None:
+            g = self._graphs[key] = self.graph(cap, waveforms=waveforms, diagnostics=diagnostics)
+        return g
+
+    def graph(self, max_sources: int, waveforms: bool = False,
+              diagnostics: bool = False) -> "BatchGraph":
+        """A CUDA graph of this plan's staging copy and kernel launch(es) for
+        up to ``max_sources`` sources of any lengths (flr_batch_graph_create).
+        ``waveforms``: the graph also generates galactic-binary waveforms
+        (use its :meth:`BatchGraph.run_gb`)."""
+        return BatchGraph(self, max_sources, waveforms, diagnostics)
 
     def status(self, reset: bool = False) -> int:
         """Kernel status bits (see include/flr_gb300.h; 0x10 = a staging copy
         did not complete); synchronises."""
         return self.cpp_orbits.status(reset=reset)
+
+
+class BatchGraph:
+    """A captured batch launch of a :class:`BatchedResponseTDI` plan for up to
+    ``max_sources`` sources of any lengths.  Calls take the same arguments as
+    the plan's ``__call__`` / ``run_gb`` and give bit-identical results; each
+    replays the graph after staging the sources (two staging buffers
+    alternate, so a call can be prepared while the previous one runs)."""
+
+    def __init__(self, owner: BatchedResponseTDI, max_sources: int, waveforms: bool,
+                 diagnostics: bool):
+        self.owner = owner
+        self.max_sources = int(max_sources)
+        self.waveforms = bool(waveforms)
+        self.diagnostics = bool(diagnostics)
+        flags = (GRAPH_WAVEFORMS if waveforms else 0) | (GRAPH_DIAGNOSTICS if diagnostics else 0)
+        lib = _plan_fns()
+        g = ctypes.c_void_p()
+        with torch.cuda.device(owner.device):
+            rc = lib.flr_batch_graph_create(owner._plan, self.max_sources, flags,
+                                            CHANNELS[owner.tdi_chan], ctypes.byref(g))
+        _lib.check(rc)
+        self._graph = g
+
+    def __call__(self, h: Sequence, lam, beta, t0=0.0, tdi_set=0, out=None, stream=None,
+                 diagnostics: bool = False):
+        if self.waveforms:
+            raise ValueError("this graph generates waveforms: use run_gb")
+        o = self.owner
+        hs = [_as_device(x, o.device, torch.complex128) for x in h]
+        self._check(len(hs))
+        return o._run(hs, None, [len(x) for x in hs], lam, beta, t0, tdi_set, out, stream,
+                      diagnostics, self)
+
+    def run_gb(self, params, lengths, lam, beta, t0=0.0, tdi_set=0, h=None, out=None,
+               stream=None):
+        if not self.waveforms:
+            raise ValueError("this graph was created without waveforms")
+        o = self.owner
+        params = np.asarray(params, dtype=np.float64).reshape(-1, 6)
+        ns = len(params)
+        self._check(ns)
+        lengths = [int(n) for n in np.broadcast_to(np.asarray(lengths, dtype=np.int64), (ns,))]
+        hs = list(h) if h is not None else [
+            torch.empty(n, dtype=torch.complex128, device=o.device) for n in lengths]
+        for i, n in enumerate(lengths):
+            if hs[i].numel() != n or hs[i].dtype != torch.complex128 or not hs[i].is_cuda:
+                raise ValueError(f"h[{i}] must be a complex128 CUDA buffer of {n} samples")
+        return o._run(hs, params, lengths, lam, beta, t0, tdi_set, out, stream, False, self), hs
+
+    def _check(self, ns):
+        if ns > self.max_sources:
+            raise ValueError(f"{ns} sources: this graph takes at most {self.max_sources}")
+
+    def close(self):
+        if getattr(self, "_graph", None) is not None:
+            _lib.lib().flr_batch_graph_destroy(self._graph)
+            self._graph = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -7,7 +7,9 @@ the GPU, admits requests against an HBM budget (each request needs its
 waveform and its three output channels, 40 bytes per sample), and packs the
 admitted requests into one launch pair per batch: an on-device waveform
 kernel followed by the persistent fused response + TDI kernel
-(:meth:`BatchedResponseTDI.run_gb`).  Batches go to ``num_streams`` CUDA
+(:meth:`BatchedResponseTDI.run_gb`), replayed from the CUDA graph of the
+batch's size bucket (sources rounded up to a power of two; lengths are free).
+Batches go to ``num_streams`` CUDA
 streams, so a batch formed from requests that arrived while others were
 running starts right away and overlaps with them on the device; memory
 returns to the budget when a batch completes.
@@ -97,7 +99,7 @@ class GpuExecutor:
     """Runs batches with one BatchedResponseTDI plan and stream per lane."""
 
     def __init__(self, sampling_frequency, orbits, order, tdi_sets, tdi_chan, precision,
-                 t_buffer, num_streams, device):
+                 t_buffer, num_streams, device, use_graphs=True):
         import torch
 
         from .batch import BatchedResponseTDI
@@ -110,6 +112,7 @@ class GpuExecutor:
                       for _ in range(num_streams)]
         self.streams = [torch.cuda.Stream(device=device) for _ in range(num_streams)]
         self.lanes = num_streams
+        self.use_graphs = use_graphs
 
     def launch(self, lane: int, batch: List[Request]):
         torch = self.torch
@@ -118,12 +121,12 @@ class GpuExecutor:
         beta = [r.params[7] for r in batch]
         s = self.streams[lane]
         with torch.cuda.device(self.device), torch.cuda.stream(s):
-            outs = [torch.zeros((3, r.n), dtype=torch.float64, device=self.device)
+            outs = [torch.empty((3, r.n), dtype=torch.float64, device=self.device)
                     for r in batch]
             hs = [torch.empty(r.n, dtype=torch.complex128, device=self.device) for r in batch]
             self.plans[lane].run_gb(params, [r.n for r in batch], lam, beta,
                                     t0=[r.t0 for r in batch], tdi_set=[r.tdi_set for r in batch],
-                                    h=hs, out=outs, stream=s)
+                                    h=hs, out=outs, stream=s, use_graph=self.use_graphs)
             ev = torch.cuda.Event()
             ev.record(s)
         return (ev, outs, hs)
