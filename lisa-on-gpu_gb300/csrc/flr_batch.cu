@@ -32,6 +32,7 @@
 struct flr_batch_plan {
     int device;
     bool mixed;
+    bool grouped;              // mixed, equal-arm orbits, every set in grouped form
     flr::FusedArgs base;
     size_t smem;
     int grid_max;
@@ -100,6 +101,43 @@ void release(flr_batch_plan *p) {
     if (p->stage_free) cudaEventDestroy(p->stage_free);
     if (p->done) cudaEventDestroy(p->done);
     delete p;
+}
+
+// Grouped form of a set whose units are ordered by delay-list length (mixed
+// arithmetic, equal-arm orbits): runs of equal length become groups, and per
+// group and channel the units' signed base links are merged into at most two
+// link rows with coefficients +-1.  Leaves grouped = 0 when a set does not fit.
+void make_groups(flr::FusedTdiSet &s) {
+    s.grouped = 0;
+    int ng = 0;
+    for (int u = 0; u < s.num_units;) {
+        int v = u;
+        while (v < s.num_units && s.delay_len[v] == s.delay_len[u]) ++v;
+        if (ng == flr::kFusedMaxGroups) return;
+        double coef[3][6] = {};
+        for (int w = u; w < v; ++w) coef[s.channel[w]][s.base_slot[w]] += s.sign[w];
+        s.group_len[ng] = s.delay_len[u];
+        s.group_start[ng] = u;
+        for (int c = 0; c < 3; ++c) {
+            int terms = 0;
+            for (int q = 0; q < 2; ++q) {
+                s.group_row[ng][c][q] = 0;
+                s.group_sign[ng][c][q] = 0.f;
+            }
+            for (int slot = 0; slot < 6; ++slot) {
+                if (coef[c][slot] == 0.0) continue;
+                if (terms == 2 || (coef[c][slot] != 1.0 && coef[c][slot] != -1.0)) return;
+                s.group_row[ng][c][terms] = slot;
+                s.group_sign[ng][c][terms] = (float)coef[c][slot];
+                ++terms;
+            }
+        }
+        ++ng;
+        u = v;
+    }
+    s.group_start[ng] = s.num_units;
+    s.num_groups = ng;
+    s.grouped = 1;
 }
 
 // Staging layout: descriptors | tile prefix sums | waveform parameters |
@@ -206,7 +244,7 @@ cudaError_t enqueue(const flr_batch_plan *plan, const unsigned char *h_stage,
     a.tile_start = reinterpret_cast<const long *>(d_stage + lay.tiles);
     a.num_sources = cap;
     a.chan = chan;
-    return flr::launch_fused(plan->mixed, diag, a, plan->grid_max, plan->smem, st);
+    return flr::launch_fused(plan->mixed, plan->grouped, diag, a, plan->grid_max, plan->smem, st);
 }
 
 void release_graph(flr_batch_graph *g) {
@@ -338,12 +376,17 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
             s.prefix_keep[u] = keep;
             max_len = std::max(max_len, len);
         }
+        if (mixed && equal_arms) make_groups(s);
     }
+    const bool grouped =
+        mixed && equal_arms &&
+        std::all_of(hsets.begin(), hsets.end(), [](const flr::FusedTdiSet &t) { return t.grouped; });
 
 
     flr_batch_plan *p = new flr_batch_plan();
     p->device = orbits->device;
     p->mixed = mixed;
+    p->grouped = grouped;
     p->num_sets = num_sets;
     p->set_max_len = max_len;
     const int y_halo = (int)std::ceil(max_len * lmax * sampling_frequency) + h + 3;
@@ -398,7 +441,7 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
                                            std::to_string(smem_optin));
     }
     int per_sm = 0;
-    if (err == cudaSuccess) err = flr::fused_configure(p->mixed, p->smem, &per_sm);
+    if (err == cudaSuccess) err = flr::fused_configure(p->mixed, p->grouped, p->smem, &per_sm);
     int sms = 0;
     if (err == cudaSuccess)
         err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
@@ -445,7 +488,8 @@ int flr_batch_plan_info(const flr_batch_plan *plan, int *info, int n_info) {
     if (!plan || !info) return fail(FLR_E_INVALID_ARGUMENT, "NULL argument");
     const int vals[] = {plan->base.tile, plan->base.y_halo, plan->base.win_max,
                         plan->base.y_max, (int)plan->smem, plan->grid_max,
-                        plan->mixed ? FLR_PRECISION_MIXED : FLR_PRECISION_FP64};
+                        plan->mixed ? FLR_PRECISION_MIXED : FLR_PRECISION_FP64,
+                        plan->grouped ? 1 : 0};
     for (int i = 0; i < n_info && i < (int)(sizeof(vals) / sizeof(int)); ++i) info[i] = vals[i];
     return FLR_OK;
 }

@@ -356,10 +356,61 @@ __device__ __forceinline__ df::f2 df_interp_real(const float2 *y, int d, df::f2 
     return df::acc_value(acc);
 }
 
+// Output sample i of the channels: X, Y, Z or lisaanalysistools' AET,
+// (Z-X)/sqrt2, (X-2Y+Z)/sqrt6, (X+Y+Z)/sqrt3 (AE: a zero third row).
+__device__ __forceinline__ void store_channels(double *out, long n, long i, int chan, double X,
+                                               double Yc, double Z) {
+    if (chan == kChanXYZ) {
+        out[i] = X;
+        out[n + i] = Yc;
+        out[2 * n + i] = Z;
+    } else {
+        out[i] = (Z - X) / 1.4142135623730951;
+        out[n + i] = (X - 2.0 * Yc + Z) / 2.449489742783178;
+        out[2 * n + i] = (chan == kChanAET) ? (X + Yc + Z) / 1.7320508075688772 : 0.0;
+    }
+}
+
+// Grouped real interpolation: for each channel c the interpolation at one
+// delay (d, eps) of the row combination s0 y[r0] + s1 y[r1] (rows at shared
+// offsets off[c][*], signs sg[c][*] in {-1, 0, +1}); the weights are computed
+// once for the three channels.
+__device__ __forceinline__ void df_interp_group(const float2 *y, const int off[3][2],
+                                                const float sg[3][2], int d, df::f2 A,
+                                                df::f2 eps, const df::f2 *edf, int h,
+                                                df::f2 out[3]) {
+    const DfWeights w = df_weights(A, eps);
+    df::Acc acc[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) df::acc_init(acc[c]);
+    auto tap = [&](df::f2 W, int k) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float2 v0 = y[off[c][0] + k], v1 = y[off[c][1] + k];
+            const df::f2 z = df::add({sg[c][0] * v0.x, sg[c][0] * v0.y},
+                                     {sg[c][1] * v1.x, sg[c][1] * v1.y});
+            df::acc_fma(acc[c], W, z);
+        }
+    };
+    tap(df::mul_raw(w.A, w.ome), d + 1);
+    tap(df::mul_raw(w.A, w.e), d);
+    for (int j = 1; j < h; ++j) {
+        const df::f2 cE = df::mul(w.c, edf[j - 1]);
+        tap(df::mul_raw(cE, df::rcp(df::add_big_float((float)j, w.e))), d + 1 + j);
+        tap(df::mul_raw(cE, df::rcp(df::add_big_float((float)j, w.ome))), d - j);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) out[c] = df::acc_value(acc[c]);
+}
+
 // -------------------------------------------------------------- the kernel ----
 
-template <bool kMixed, bool kDiag>
+// Register budgets are the compiler's own choice: pinning the grouped
+// instance to three blocks per SM (80 registers) measured 2.5 % slower than
+// its unbounded 128 registers at two blocks per SM.
+template <bool kMixed, bool kDiag, bool kGrouped>
 __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
+    static_assert(kMixed || !kGrouped, "the grouped form is a mixed-arithmetic form");
     extern __shared__ __align__(128) unsigned char smem[];
     const Layout lay = layout(kMixed, a.win_max, a.y_max);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
@@ -613,97 +664,140 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
 
         // 5. TDI for the output samples [o0, o1)
         const double inv_scale = 1.0 / scale;
-        for (long i = o0 + tid; i < o1; i += kThreads) {
-            const double t = t0 + (double)i * a.dt;
-            double L[kLinks];
-            if (kMixed) {
+        if (kGrouped) {
+            for (long i = o0 + tid; i < o1; i += kThreads) {
+                const double t = t0 + (double)i * a.dt;
                 const int w = orbit_segment_fast(a.orb, a.inv_orbit_dt, t);
+                // every link has this L(t): the delay of a list of length m is t - L - ... - L
+                const double L0 =
+                    (w < 0) ? 0.0 : orbit_lerp(a.orb.ltt, a.orb.ltt_slope, w, 6, 0, t, a.orb.dt);
+                df::f2 accdf[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+                double delay = t;
+                int depth = 0;
+                for (int g = 0; g < set->num_groups; ++g) {
+                    for (const int len = set->group_len[g]; depth < len; ++depth)
+                        delay = delay - L0;
+                    int d;
+                    double eps;
+                    split_delay_fast(delay, t0, a.fs, d, eps);
+                    if (kDiag && src.d_tdi_out)
+                        for (int u = set->group_start[g]; u < set->group_start[g + 1]; ++u)
+                            src.d_tdi_out[(long)set->orig_unit[u] * n + i] = d;
+                    const long lo = (long)d - (h - 1), hi = (long)d + h;
+                    if (lo < ya || hi >= yb) {
+                        raise_status(a.orb.status, kStatusTap);
 #pragma unroll
-                for (int s = 0; s < kLinks; ++s)
-                    L[s] = (w < 0) ? 0.0 : orbit_lerp(a.orb.ltt, a.orb.ltt_slope, w, 6, s, t,
-                                                      a.orb.dt);
-            } else {
-#pragma unroll
-                for (int s = 0; s < kLinks; ++s) L[s] = light_travel_time(a.orb, t, s);
-            }
-            double acc64[3] = {0.0, 0.0, 0.0};
-            df::f2 accdf[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-            double stack[kFusedMaxDepth + 1];  // partial delays t - L_1 - ... - L_s
-            stack[0] = t;
-            long long prev_bits = 0x7ff8dead00000000ll;  // a NaN no delay can equal
-            int d = 0;
-            double eps = 0.0;
-            df::f2 e_df = {0.f, 0.f}, A_df = {0.f, 0.f};
-            for (int unit = 0; unit < set->num_units; ++unit) {
-                const int ch = set->channel[unit];
-                const int len = set->delay_len[unit];
-                for (int s = set->prefix_keep[unit]; s < len; ++s)
-                    stack[s + 1] = stack[s] - L[set->delay_slot[unit][s]];
-                const double delay = stack[len];
-                if (kMixed) {
-                    // consecutive units with bit-identical delays share the split
-                    const long long bits = __double_as_longlong(delay);
-                    if (bits != prev_bits) {
-                        split_delay_fast(delay, t0, a.fs, d, eps);
-                        e_df = df::from_double(eps);
-                        A_df = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_df);
-                        prev_bits = bits;
-                    }
-                } else {
-                    split_delay(delay, t0, a.fs, d, eps);
-                }
-                if (kDiag && src.d_tdi_out) src.d_tdi_out[(long)set->orig_unit[unit] * n + i] = d;
-                const int b = set->base_slot[unit];
-                const long lo = (long)d - (h - 1), hi = (long)d + h;
-                if (lo < ya || hi >= yb) {
-                    raise_status(a.orb.status, kStatusTap);
-                    acc64[ch] = qnan();
-                    accdf[ch] = {__int_as_float(0x7fc00000), 0.f};
-                    continue;
-                }
-                if (kMixed) {
-                    df::f2 val = df_interp_real(y32 + b * a.y_max, (int)(d - ya), A_df, e_df, edf,
-                                                h);
-                    const int sc = set->sign_code[unit];
-                    if (sc == 1)
-                        accdf[ch] = df::add(accdf[ch], val);
-                    else if (sc == -1)
-                        accdf[ch] = df::sub(accdf[ch], val);
-                    else
-                        accdf[ch] = df::add(accdf[ch], df::mul(val, df::from_double(set->sign[unit])));
-                } else {
-                    double pre;
-                    if (!prefactor(a.lt, eps, pre)) {
-                        raise_status(a.orb.status, kStatusAIndex);
-                        acc64[ch] = qnan();
+                        for (int c = 0; c < 3; ++c)
+                            if (set->group_sign[g][c][0] != 0.f || set->group_sign[g][c][1] != 0.f)
+                                accdf[c] = {__int_as_float(0x7fc00000), 0.f};
                         continue;
                     }
-                    const SharedF64 row{y64 + b * a.y_max};
-                    double val = lagrange_real(row, (int)(d - ya), eps, pre, a.lt);
-                    val *= set->sign[unit];
-                    acc64[ch] += val;
+                    int off[3][2];
+                    float sg[3][2];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+#pragma unroll
+                        for (int q = 0; q < 2; ++q) {
+                            off[c][q] = set->group_row[g][c][q] * a.y_max;
+                            sg[c][q] = set->group_sign[g][c][q];
+                        }
+                    const df::f2 e_df = df::from_double(eps);
+                    const df::f2 A_df = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_df);
+                    df::f2 val[3];
+                    df_interp_group(y32, off, sg, (int)(d - ya), A_df, e_df, edf, h, val);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) accdf[c] = df::add(accdf[c], val[c]);
                 }
+                const double X = df::to_double(accdf[0]) * inv_scale;
+                const double Yc = df::to_double(accdf[1]) * inv_scale;
+                const double Z = df::to_double(accdf[2]) * inv_scale;
+                store_channels(src.out, n, i, a.chan, X, Yc, Z);
             }
-            double X, Yc, Z;
-            if (kMixed) {
-                X = df::to_double(accdf[0]) * inv_scale;
-                Yc = df::to_double(accdf[1]) * inv_scale;
-                Z = df::to_double(accdf[2]) * inv_scale;
-            } else {
-                X = acc64[0];
-                Yc = acc64[1];
-                Z = acc64[2];
-            }
-            double *out = src.out;
-            if (a.chan == kChanXYZ) {
-                out[i] = X;
-                out[n + i] = Yc;
-                out[2 * n + i] = Z;
-            } else {
-                // lisaanalysistools AET: (Z-X)/sqrt2, (X-2Y+Z)/sqrt6, (X+Y+Z)/sqrt3
-                out[i] = (Z - X) / 1.4142135623730951;
-                out[n + i] = (X - 2.0 * Yc + Z) / 2.449489742783178;
-                out[2 * n + i] = (a.chan == kChanAET) ? (X + Yc + Z) / 1.7320508075688772 : 0.0;
+        } else {
+            for (long i = o0 + tid; i < o1; i += kThreads) {
+                const double t = t0 + (double)i * a.dt;
+                double L[kLinks];
+                if (kMixed) {
+                    const int w = orbit_segment_fast(a.orb, a.inv_orbit_dt, t);
+#pragma unroll
+                    for (int s = 0; s < kLinks; ++s)
+                        L[s] = (w < 0) ? 0.0 : orbit_lerp(a.orb.ltt, a.orb.ltt_slope, w, 6, s, t,
+                                                          a.orb.dt);
+                } else {
+#pragma unroll
+                    for (int s = 0; s < kLinks; ++s) L[s] = light_travel_time(a.orb, t, s);
+                }
+                double acc64[3] = {0.0, 0.0, 0.0};
+                df::f2 accdf[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+                double stack[kFusedMaxDepth + 1];  // partial delays t - L_1 - ... - L_s
+                stack[0] = t;
+                long long prev_bits = 0x7ff8dead00000000ll;  // a NaN no delay can equal
+                int d = 0;
+                double eps = 0.0;
+                df::f2 e_df = {0.f, 0.f}, A_df = {0.f, 0.f};
+                for (int unit = 0; unit < set->num_units; ++unit) {
+                    const int ch = set->channel[unit];
+                    const int len = set->delay_len[unit];
+                    for (int s = set->prefix_keep[unit]; s < len; ++s)
+                        stack[s + 1] = stack[s] - L[set->delay_slot[unit][s]];
+                    const double delay = stack[len];
+                    if (kMixed) {
+                        // consecutive units with bit-identical delays share the split
+                        const long long bits = __double_as_longlong(delay);
+                        if (bits != prev_bits) {
+                            split_delay_fast(delay, t0, a.fs, d, eps);
+                            e_df = df::from_double(eps);
+                            A_df = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_df);
+                            prev_bits = bits;
+                        }
+                    } else {
+                        split_delay(delay, t0, a.fs, d, eps);
+                    }
+                    if (kDiag && src.d_tdi_out)
+                        src.d_tdi_out[(long)set->orig_unit[unit] * n + i] = d;
+                    const int b = set->base_slot[unit];
+                    const long lo = (long)d - (h - 1), hi = (long)d + h;
+                    if (lo < ya || hi >= yb) {
+                        raise_status(a.orb.status, kStatusTap);
+                        acc64[ch] = qnan();
+                        accdf[ch] = {__int_as_float(0x7fc00000), 0.f};
+                        continue;
+                    }
+                    if (kMixed) {
+                        df::f2 val =
+                            df_interp_real(y32 + b * a.y_max, (int)(d - ya), A_df, e_df, edf, h);
+                        const int sc = set->sign_code[unit];
+                        if (sc == 1)
+                            accdf[ch] = df::add(accdf[ch], val);
+                        else if (sc == -1)
+                            accdf[ch] = df::sub(accdf[ch], val);
+                        else
+                            accdf[ch] = df::add(accdf[ch],
+                                                df::mul(val, df::from_double(set->sign[unit])));
+                    } else {
+                        double pre;
+                        if (!prefactor(a.lt, eps, pre)) {
+                            raise_status(a.orb.status, kStatusAIndex);
+                            acc64[ch] = qnan();
+                            continue;
+                        }
+                        const SharedF64 row{y64 + b * a.y_max};
+                        double val = lagrange_real(row, (int)(d - ya), eps, pre, a.lt);
+                        val *= set->sign[unit];
+                        acc64[ch] += val;
+                    }
+                }
+                double X, Yc, Z;
+                if (kMixed) {
+                    X = df::to_double(accdf[0]) * inv_scale;
+                    Yc = df::to_double(accdf[1]) * inv_scale;
+                    Z = df::to_double(accdf[2]) * inv_scale;
+                } else {
+                    X = acc64[0];
+                    Yc = acc64[1];
+                    Z = acc64[2];
+                }
+                store_channels(src.out, n, i, a.chan, X, Yc, Z);
             }
         }
         __syncthreads();
@@ -716,31 +810,34 @@ size_t fused_smem_bytes(bool mixed, int win_max, int y_max) {
     return layout(mixed, win_max, y_max).total;
 }
 
-static const void *fused_fn(bool mixed, bool diag) {
-    if (diag)
-        return mixed ? reinterpret_cast<const void *>(fused_kernel<true, true>)
-                     : reinterpret_cast<const void *>(fused_kernel<false, true>);
-    return mixed ? reinterpret_cast<const void *>(fused_kernel<true, false>)
-                 : reinterpret_cast<const void *>(fused_kernel<false, false>);
+static const void *fused_fn(bool mixed, bool grouped, bool diag) {
+    if (mixed && grouped)
+        return diag ? reinterpret_cast<const void *>(fused_kernel<true, true, true>)
+                    : reinterpret_cast<const void *>(fused_kernel<true, false, true>);
+    if (mixed)
+        return diag ? reinterpret_cast<const void *>(fused_kernel<true, true, false>)
+                    : reinterpret_cast<const void *>(fused_kernel<true, false, false>);
+    return diag ? reinterpret_cast<const void *>(fused_kernel<false, true, false>)
+                : reinterpret_cast<const void *>(fused_kernel<false, false, false>);
 }
 
-cudaError_t fused_configure(bool mixed, size_t smem_bytes, int *blocks_per_sm) {
+cudaError_t fused_configure(bool mixed, bool grouped, size_t smem_bytes, int *blocks_per_sm) {
     for (bool diag : {true, false}) {
-        cudaError_t err = cudaFuncSetAttribute(fused_fn(mixed, diag),
+        cudaError_t err = cudaFuncSetAttribute(fused_fn(mixed, grouped, diag),
                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)smem_bytes);
         if (err != cudaSuccess) return err;
     }
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fused_fn(mixed, false),
-                                                         kThreads, smem_bytes);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        blocks_per_sm, fused_fn(mixed, grouped, false), kThreads, smem_bytes);
 }
 
-cudaError_t launch_fused(bool mixed, bool diag, const FusedArgs &a, int grid, size_t smem_bytes,
-                         cudaStream_t stream) {
+cudaError_t launch_fused(bool mixed, bool grouped, bool diag, const FusedArgs &a, int grid,
+                         size_t smem_bytes, cudaStream_t stream) {
     if (a.num_sources <= 0) return cudaSuccess;
     void *args[] = {const_cast<FusedArgs *>(&a)};
-    return cudaLaunchKernel(fused_fn(mixed, diag), dim3(grid), dim3(kThreads), args, smem_bytes,
-                            stream);
+    return cudaLaunchKernel(fused_fn(mixed, grouped, diag), dim3(grid), dim3(kThreads), args,
+                            smem_bytes, stream);
 }
 
 }  // namespace flr

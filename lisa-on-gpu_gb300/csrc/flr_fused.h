@@ -11,6 +11,7 @@ constexpr int kFusedMaxUnits = 64;
 constexpr int kFusedMaxCombos = 320;
 constexpr int kFusedMaxDepth = 16;  // links per TDI delay list
 constexpr int kFusedMaxH = 40;   // h = (order + 1) / 2 supported by the fused kernel
+constexpr int kFusedMaxGroups = kFusedMaxDepth + 1;  // distinct delay-list lengths
 
 // One source of a batch (device copy of flr_batch_source plus derived values).
 struct FusedSource {
@@ -49,6 +50,22 @@ struct FusedTdiSet {
     int orig_unit[kFusedMaxUnits];    // position of the unit in the caller's table
     int delay_slot[kFusedMaxUnits][kFusedMaxDepth];
     int combo_slot[kFusedMaxCombos];  // -1: no delay
+    // Grouped form, for mixed arithmetic on equal-arm orbits, where every L(t)
+    // is the same value and units with delay lists of equal length have
+    // bitwise-equal delays.  Group g holds the units [group_start[g],
+    // group_start[g + 1]) (lists of length group_len[g], ascending) and adds to
+    // channel c the interpolation, at that one delay, of the signed link-row
+    // combination group_sign[g][c][0] y[group_row[g][c][0]] +
+    // group_sign[g][c][1] y[group_row[g][c][1]] (a sign of 0 marks an unused
+    // term): by linearity the sum of the units' interpolations.  grouped = 0
+    // when the set does not take this form (more than two links or a
+    // coefficient other than +-1 in some group and channel).
+    int grouped;
+    int num_groups;
+    int group_len[kFusedMaxGroups];
+    int group_start[kFusedMaxGroups + 1];
+    int group_row[kFusedMaxGroups][3][2];
+    float group_sign[kFusedMaxGroups][3][2];
 };
 
 enum FusedChan { kChanXYZ = 0, kChanAET = 1, kChanAE = 2 };
@@ -90,9 +107,11 @@ cudaError_t launch_gb_waveforms(const FusedSource *src, const GbParams *par,
                                 cudaStream_t stream);
 
 size_t fused_smem_bytes(bool mixed, int win_max, int y_max);
-cudaError_t fused_configure(bool mixed, size_t smem_bytes, int *blocks_per_sm);
+// grouped: the mixed instance for sets in grouped form (every set of the plan).
+cudaError_t fused_configure(bool mixed, bool grouped, size_t smem_bytes, int *blocks_per_sm);
 // diag: the instance that writes the FusedSource diagnostics (more registers).
-cudaError_t launch_fused(bool mixed, bool diag, const FusedArgs &a, int grid, size_t smem_bytes,
+cudaError_t launch_fused(bool mixed, bool grouped, bool diag, const FusedArgs &a, int grid,
+                         size_t smem_bytes,
                          cudaStream_t stream);
 
 }  // namespace flr

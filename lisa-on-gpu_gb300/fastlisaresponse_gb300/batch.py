@@ -202,10 +202,10 @@ class BatchedResponseTDI:
         _lib.check(rc)
         self._plan = plan
         self._graphs = {}
-        info = (ctypes.c_int * 7)()
-        lib.flr_batch_plan_info(plan, info, 7)
+        info = (ctypes.c_int * 8)()
+        lib.flr_batch_plan_info(plan, info, 8)
         self.plan_info = dict(zip(("tile", "y_halo", "win_max", "y_max", "smem_bytes",
-                                   "grid", "precision"), list(info)))
+                                   "grid", "precision", "grouped"), list(info)))
 
     def __del__(self):
         try:

@@ -74,22 +74,26 @@ def test_batch_fp64_many_sources_match_plain(gpu_lib):
         assert np.array_equal(_np(outs[i]), want), f"source {i}"
 
 
+@pytest.mark.parametrize("orbit_kind", ["kepler", "equal"])
 @pytest.mark.parametrize("order", [25, 45])
 @pytest.mark.parametrize("gen", ["1st generation", "2nd generation"])
-def test_batch_mixed_accuracy(gpu_lib, order, gen):
-    """Mixed precision against FP64 over 1e-4..1e-2 Hz, flexing orbits."""
+def test_batch_mixed_accuracy(gpu_lib, order, gen, orbit_kind):
+    """Mixed precision against FP64 over 1e-4..1e-2 Hz; flexing orbits (per-unit
+    TDI) and equal-arm orbits (TDI units in equal-delay groups)."""
     import fastlisaresponse_gb300 as flr
 
     dt = 10.0
     f = [1e-4, 3e-4, 1e-3, 3e-3, 1e-2]
     lengths = [40000] * len(f)
-    orb = flr.KeplerianOrbits(t_max=8e5)
+    orb = flr.KeplerianOrbits(t_max=8e5) if orbit_kind == "kepler" else \
+        flr.EqualArmlengthOrbits(t_max=8e5)
     hs, lam, beta, t0 = _sources(orb, dt, lengths, seed=11, f=f)
     tb = 1e4 if order <= 25 else 2e4  # order 45 needs the longer garbage margin
     ref = flr.BatchedResponseTDI(1 / dt, order=order, tdi=gen, orbits=orb, precision="fp64",
                                  t_buffer=tb)
     mix = flr.BatchedResponseTDI(1 / dt, order=order, tdi=gen, orbits=orb, precision="mixed",
                                  t_buffer=tb)
+    assert mix.plan_info["grouped"] == (orbit_kind == "equal")
     want = [_np(o) for o in ref(hs, lam, beta, t0=t0)]
     got = [_np(o) for o in mix(hs, lam, beta, t0=t0)]
     assert mix.status() == 0
@@ -146,3 +150,28 @@ def test_batch_indices_and_links_match_plain(gpu_lib, orbit_kind, precision):
         else:
             for link in range(6):
                 assert rel_l2(y_fused[link], y_plain[link]) <= MIXED_TOL
+
+
+@pytest.mark.parametrize("chan", ["AET", "AE"])
+def test_batch_mixed_grouped_channels_and_sets(gpu_lib, chan):
+    """Equal-arm orbits, two TDI sets in one launch, AET / AE outputs: the
+    grouped mixed path against FP64 per channel."""
+    import fastlisaresponse_gb300 as flr
+
+    dt = 10.0
+    orb = flr.EqualArmlengthOrbits(t_max=1.2e6)
+    lengths = [3000, 30000, 77777, 12000]
+    hs, lam, beta, t0 = _sources(orb, dt, lengths, seed=13)
+    sets = [0, 1, 1, 0]
+    kw = dict(order=25, tdi=["1st generation", "2nd generation"], orbits=orb, tdi_chan=chan)
+    ref = flr.BatchedResponseTDI(1 / dt, precision="fp64", **kw)
+    mix = flr.BatchedResponseTDI(1 / dt, precision="mixed", **kw)
+    assert mix.plan_info["grouped"] == 1
+    want = [_np(o) for o in ref(hs, lam, beta, t0=t0, tdi_set=sets)]
+    got = [_np(o) for o in mix(hs, lam, beta, t0=t0, tdi_set=sets)]
+    assert mix.status() == 0
+    for i in range(len(lengths)):
+        for c in range(2):
+            assert rel_l2(got[i][c], want[i][c]) <= MIXED_TOL
+        if chan == "AE":
+            assert not np.any(got[i][2])
