@@ -157,21 +157,63 @@ __device__ __forceinline__ void position_seg(const OrbitTables &o, int w, double
     for (int c = 0; c < 3; ++c) out[c] = orbit_lerp(o.x, o.x_slope, w, 9, 3 * s + c, t, o.dt);
 }
 
-// The reference's index split (LISAResponse.cu:339-341, 616-622),
-// d = (int)ceil(y) - 1 and eps = (1 + d) - y with y = (t - t0) * fs, with the
-// ceiling taken by a round-up conversion: (double)(d + 1) equals 1.0 + d, so
-// d and eps are bit-identical to split_delay().
-__device__ __forceinline__ void split_delay_fast(double delayed_t, double t_first, double fs,
-                                                 int &d, double &eps) {
-    const double y = (delayed_t - t_first) * fs;
-    const int c = __double2int_ru(y);
+// K * 2^-fb as a df value, for 0 < K < 2^fb and 22 <= fb <= 52: the floats
+// are assembled from the bits of K (hi = its top 24 significant bits, lo the
+// rest, truncated to 24 bits), so no FP64 or conversion instruction is used.
+// Exact when K has at most 48 significant bits.
+__device__ __forceinline__ df::f2 df_from_fixed(unsigned long long K, int fb) {
+    const int len = 64 - __clzll((long long)K);  // 1..52
+    const int sh = len - 24;
+    const unsigned long long top = (sh >= 0) ? (K >> sh) : (K << -sh);
+    const float hi = __int_as_float(((len - 1 - fb + 127) << 23) | (int)(top & 0x7fffffu));
+    float lo = 0.f;
+    if (sh > 0) {
+        const unsigned long long rest = K & ((1ull << sh) - 1);
+        if (rest != 0) {
+            const int len2 = 64 - __clzll((long long)rest);
+            const int sh2 = len2 - 24;
+            const unsigned long long top2 = (sh2 >= 0) ? (rest >> sh2) : (rest << -sh2);
+            lo = __int_as_float(((len2 - 1 - fb + 127) << 23) | (int)(top2 & 0x7fffffu));
+        }
+    }
+    return {hi, lo};
+}
+
+// The mixed flavour's index split.  The reference's (LISAResponse.cu:339-341,
+// 616-622) is d = (int)ceil(x) - 1, eps = (1 + d) - x for x = (t - t0) * fs,
+// x computed in FP64 with the same operations; (1 + d) - x is exact, so eps is
+// determined by the bits of x.  For 1 <= x < 2^31 the integer and fractional
+// parts are read from those bits (x = (m >> fb) + (m & (2^fb - 1)) 2^-fb for
+// the significand m and fb = 52 - exponent): the same d and the same value of
+// eps, as a df, without FP64 conversions.  Other x take the FP64 route, the
+// ceiling as a round-up conversion ((double)(d + 1) equals 1.0 + d).
+__device__ __forceinline__ void split_delay_df(double delayed_t, double t_first, double fs,
+                                               int &d, df::f2 &eps) {
+    const double x = (delayed_t - t_first) * fs;
+    const long long b = __double_as_longlong(x);
+    const int e = (int)(b >> 52) - 1023;  // negative x: e < -1023
+    if (e >= 0 && e <= 30) {
+        const int fb = 52 - e;
+        const unsigned long long m = ((unsigned long long)b & 0xfffffffffffffull) | (1ull << 52);
+        const unsigned long long frac = m & ((1ull << fb) - 1);
+        const int ip = (int)(m >> fb);
+        if (frac != 0) {
+            d = ip;
+            eps = df_from_fixed((1ull << fb) - frac, fb);
+        } else {
+            d = ip - 1;
+            eps = {0.f, 0.f};
+        }
+        return;
+    }
+    const int c = __double2int_ru(x);
     d = c - 1;
-    eps = (double)c - y;
+    eps = df::from_double((double)c - x);
 }
 
 struct MixedDelays {
     int d_rec, d_em;
-    double e_rec, e_em;
+    df::f2 e_rec, e_em;
     double x_rec[3], x_em[3];
 };
 
@@ -189,8 +231,8 @@ __device__ __forceinline__ MixedDelays link_delays_mixed(const OrbitTables &o, d
     position_seg(o, orbit_segment_fast(o, inv_dt, t_em), t_em, o.sc_e[slot], g.x_em);
     double kx_rec = dot3(k, g.x_rec);
     double kx_em = dot3(k, g.x_em);
-    split_delay_fast(t - kx_rec * kCInv, t_first, fs, g.d_rec, g.e_rec);
-    split_delay_fast(t_em - kx_em * kCInv, t_first, fs, g.d_em, g.e_em);
+    split_delay_df(t - kx_rec * kCInv, t_first, fs, g.d_rec, g.e_rec);
+    split_delay_df(t_em - kx_em * kCInv, t_first, fs, g.d_em, g.e_em);
     return g;
 }
 
@@ -599,7 +641,7 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
                 }
                 const long lo = (long)min(g.d_rec, g.d_em) - (h - 1);
                 const long hi = (long)max(g.d_rec, g.d_em) + h;
-                const df::f2 e_r = df::from_double(g.e_rec), e_e = df::from_double(g.e_em);
+                const df::f2 e_r = g.e_rec, e_e = g.e_em;
                 const df::f2 A_r = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_r);
                 const df::f2 A_e = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_e);
                 df::f2 re_r, im_r, re_e, im_e;
@@ -678,8 +720,8 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
                     for (const int len = set->group_len[g]; depth < len; ++depth)
                         delay = delay - L0;
                     int d;
-                    double eps;
-                    split_delay_fast(delay, t0, a.fs, d, eps);
+                    df::f2 e_df;
+                    split_delay_df(delay, t0, a.fs, d, e_df);
                     if (kDiag && src.d_tdi_out)
                         for (int u = set->group_start[g]; u < set->group_start[g + 1]; ++u)
                             src.d_tdi_out[(long)set->orig_unit[u] * n + i] = d;
@@ -701,7 +743,6 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
                             off[c][q] = set->group_row[g][c][q] * a.y_max;
                             sg[c][q] = set->group_sign[g][c][q];
                         }
-                    const df::f2 e_df = df::from_double(eps);
                     const df::f2 A_df = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_df);
                     df::f2 val[3];
                     df_interp_group(y32, off, sg, (int)(d - ya), A_df, e_df, edf, h, val);
@@ -745,8 +786,7 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
                         // consecutive units with bit-identical delays share the split
                         const long long bits = __double_as_longlong(delay);
                         if (bits != prev_bits) {
-                            split_delay_fast(delay, t0, a.fs, d, eps);
-                            e_df = df::from_double(eps);
+                            split_delay_df(delay, t0, a.fs, d, e_df);
                             A_df = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_df);
                             prev_bits = bits;
                         }
