@@ -280,7 +280,10 @@ __device__ __forceinline__ DfProjection df_projection(const double x_rec[3], con
 // by rounding only.
 __device__ __forceinline__ df::f2 prefactor_df(const float4 *tab, int num_A, df::f2 inv_deps,
                                                df::f2 e) {
-    const df::f2 q = df::mul_raw(e, inv_deps);
+    // normalised, so that |q.lo| <= ulp(q.hi) / 2 and floor(q.hi) (corrected
+    // below when q.hi is a knot) is the segment of q itself: a q.hi a few
+    // ulp under a knot would pick the previous segment and extrapolate it
+    const df::f2 q = df::renorm(df::mul_raw(e, inv_deps));
     const float fl = floorf(q.hi);
     int ind = (int)fl;
     if (q.hi == fl && q.lo < 0.f) ind -= 1;

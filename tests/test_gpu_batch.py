@@ -13,6 +13,7 @@ from conftest import TableOrbits, golden_names, load_golden, rel_l2
 pytestmark = pytest.mark.gpu
 
 MIXED_TOL = 1e-6
+LINK_TOL = 5e-12
 
 
 def _np(x):
@@ -148,8 +149,11 @@ def test_batch_indices_and_links_match_plain(gpu_lib, orbit_kind, precision):
         if precision == "fp64":
             assert np.array_equal(y_fused, y_plain)
         else:
+            # the link streams carry no TDI cancellation: double-float taps give
+            # ~1e-13; LINK_TOL guards that level (the channel bound is MIXED_TOL)
             for link in range(6):
-                assert rel_l2(y_fused[link], y_plain[link]) <= MIXED_TOL
+                err = rel_l2(y_fused[link], y_plain[link])
+                assert err <= LINK_TOL, f"source {i} link {link}: rel L2 {err:.2e}"
 
 
 @pytest.mark.parametrize("chan", ["AET", "AE"])
