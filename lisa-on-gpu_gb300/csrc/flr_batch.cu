@@ -472,6 +472,18 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
     b.dt = 1.0 / sampling_frequency;
     b.inv_deps = 1.0 / deps;
     b.inv_orbit_dt = 1.0 / orbits->dt;
+    // receiving spacecraft and their two links each (any LISA link table)
+    b.rx_shared = 1;
+    for (int r = 0; r < 3; ++r) {
+        int found = 0;
+        for (int slot = 0; slot < 6; ++slot) {
+            if (orbits->sc_r[slot] != r + 1) continue;
+            if (found < 2) b.rx_slot[r][found] = slot;
+            ++found;
+        }
+        b.rx_sc[r] = r + 1;
+        if (found != 2) b.rx_shared = 0;
+    }
     *out = p;
     return FLR_OK;
 }

@@ -236,6 +236,45 @@ __device__ __forceinline__ MixedDelays link_delays_mixed(const OrbitTables &o, d
     return g;
 }
 
+// The receiver side of link_delays_mixed(), shared by the two links a
+// spacecraft receives: its position at t and the receiver delay's split
+// (same operations as there, so the same bits).
+struct ReceiverSide {
+    int w;  // orbit segment of t
+    int d_rec;
+    df::f2 e_rec;
+    double x_rec[3];
+};
+
+__device__ __forceinline__ ReceiverSide receiver_mixed(const OrbitTables &o, double inv_dt, int sc,
+                                                       double t, double t_first, double fs,
+                                                       const double k[3]) {
+    ReceiverSide r;
+    r.w = orbit_segment_fast(o, inv_dt, t);
+    position_seg(o, r.w, t, sc, r.x_rec);
+    split_delay_df(t - dot3(k, r.x_rec) * kCInv, t_first, fs, r.d_rec, r.e_rec);
+    return r;
+}
+
+// The emitter side of link_delays_mixed() for link `slot` given the segment
+// of t: t_em = t - L(t), the emitter position at t_em and its delay's split.
+struct EmitterSide {
+    int d_em;
+    df::f2 e_em;
+    double x_em[3];
+};
+
+__device__ __forceinline__ EmitterSide emitter_mixed(const OrbitTables &o, double inv_dt, int slot,
+                                                     int w, double t, double t_first, double fs,
+                                                     const double k[3]) {
+    EmitterSide e;
+    const double L = (w < 0) ? 0.0 : orbit_lerp(o.ltt, o.ltt_slope, w, 6, slot, t, o.dt);
+    const double t_em = t - L;
+    position_seg(o, orbit_segment_fast(o, inv_dt, t_em), t_em, o.sc_e[slot], e.x_em);
+    split_delay_df(t_em - dot3(k, e.x_em) * kCInv, t_first, fs, e.d_em, e.e_em);
+    return e;
+}
+
 // 1/sqrt(x) in df: hardware approximation and one Newton step,
 // r = r0 + r0 (1 - x r0^2) / 2; relative error ~1e-14.
 __device__ __forceinline__ df::f2 df_rsqrt(df::f2 x) {
@@ -377,6 +416,25 @@ __device__ __forceinline__ void df_interp_c128_sbp(const Src &src, long d, df::f
     float4 xb = src.val(last);
     re = df::sub(df::mul(P, {xb.x, xb.y}), df::acc_value(sre));
     im = df::sub(df::mul(P, {xb.z, xb.w}), df::acc_value(sim));
+}
+
+// Complex interpolation at (d, eps) from the staged window when its taps lie
+// in it, else from global memory (the same df values); false when the taps
+// leave the input.
+__device__ __forceinline__ bool df_interp_c128_any(const float4 *hdf, const float4 *dh, long wlo,
+                                                   int W, const double2 *hg, double scale, long n,
+                                                   int d, df::f2 A, df::f2 eps, const df::f2 *edf,
+                                                   int h, df::f2 &re, df::f2 &im) {
+    const long lo = (long)d - (h - 1), hi = (long)d + h;
+    if (lo >= wlo && hi + 1 < wlo + W) {
+        df_interp_c128_sbp(DfShared{hdf, dh}, d - wlo, A, eps, edf, h, re, im);
+        return true;
+    }
+    if (lo >= 0 && hi + 1 < n) {
+        df_interp_c128_sbp(DfGlobal{hg, scale}, d, A, eps, edf, h, re, im);
+        return true;
+    }
+    return false;
 }
 
 // Real interpolation around sample d of a staged df link row, compensated dot
@@ -622,7 +680,58 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
         }
         __syncthreads();
 
-        // 4. link streams y[slot][j - ya] for j in [ya, yb)
+        // 4. link streams y[slot][j - ya] for j in [ya, yb).  Mixed flavour,
+        // two links per receiving spacecraft: one (receiver, sample) per thread
+        // iteration, the receiver's position, index split and interpolation
+        // shared by its two links (the same values the per-link form computes
+        // twice).  Otherwise one (link, sample) per thread iteration.
+        if (kMixed && a.rx_shared) {
+            for (int it = tid; it < 3 * Y; it += kThreads) {
+                const int r = it / Y;
+                const int jj = it - r * Y;
+                const long j = ya + jj;
+                if (j < yfirst || j >= ylast) {  // the reference's y_gw is zero there
+                    y32[a.rx_slot[r][0] * a.y_max + jj] = make_float2(0.f, 0.f);
+                    y32[a.rx_slot[r][1] * a.y_max + jj] = make_float2(0.f, 0.f);
+                    continue;
+                }
+                const double t = t0 + (double)j * a.dt;
+                const bool own = (j >= o0 && j < o1);  // this tile's outputs: diagnostics
+                const ReceiverSide rs =
+                    receiver_mixed(a.orb, a.inv_orbit_dt, a.rx_sc[r], t, t0, a.fs, k);
+                df::f2 re_r, im_r;
+                const bool ok_r = df_interp_c128_any(
+                    hdf, dh, wlo, W, src.h, scale, n, rs.d_rec,
+                    prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, rs.e_rec), rs.e_rec, edf, h,
+                    re_r, im_r);
+                for (int q = 0; q < 2; ++q) {
+                    const int slot = a.rx_slot[r][q];
+                    const EmitterSide es =
+                        emitter_mixed(a.orb, a.inv_orbit_dt, slot, rs.w, t, t0, a.fs, k);
+                    if (kDiag && own && src.d_rec_out) {
+                        src.d_rec_out[(long)slot * n + j] = rs.d_rec;
+                        src.d_em_out[(long)slot * n + j] = es.d_em;
+                    }
+                    df::f2 re_e, im_e;
+                    const bool ok_e = df_interp_c128_any(
+                        hdf, dh, wlo, W, src.h, scale, n, es.d_em,
+                        prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, es.e_em), es.e_em, edf, h,
+                        re_e, im_e);
+                    if (!ok_r || !ok_e) {
+                        raise_status(a.orb.status, kStatusTap);
+                        y32[slot * a.y_max + jj] = make_float2(__int_as_float(0x7fc00000), 0.f);
+                        continue;
+                    }
+                    const DfProjection pr = df_projection(rs.x_rec, es.x_em, kdf, udf, vdf);
+                    const df::f2 dre = df::sub(re_e, re_r), dim = df::sub(im_e, im_r);
+                    df::f2 yv = df::add(df::mul(dre, pr.xi_p), df::mul(dim, pr.xi_c));
+                    yv = df::mul(yv, pr.pre);
+                    y32[slot * a.y_max + jj] = make_float2(yv.hi, yv.lo);
+                    if (kDiag && own && src.y_out)
+                        src.y_out[(long)slot * n + j] = df::to_double(yv) / scale;
+                }
+            }
+        } else
         for (int it = tid; it < 6 * Y; it += kThreads) {
             const int slot = it / Y;
             const int jj = it - slot * Y;

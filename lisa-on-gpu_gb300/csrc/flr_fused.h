@@ -92,6 +92,11 @@ struct FusedArgs {
     double inv_deps;           // 1 / deps
     double inv_orbit_dt;       // 1 / orbit dt
     int chan;                  // FusedChan
+    // Receiving spacecraft: rx_sc[r] receives the links in slots rx_slot[r][0..1]
+    // (rx_shared = 1 when the orbit's six links split that way).
+    int rx_shared;
+    int rx_sc[3];
+    int rx_slot[3][2];
 };
 
 // Galactic-binary parameters of one source (on-device waveform generation).
