@@ -104,11 +104,13 @@ void release(flr_batch_plan *p) {
 }
 
 // Grouped form of a set whose units are ordered by delay-list length (mixed
-// arithmetic, equal-arm orbits): runs of equal length become groups, and per
-// group and channel the units' signed base links are merged into at most two
-// link rows with coefficients +-1.  Leaves grouped = 0 when a set does not fit.
+// arithmetic, equal-arm orbits): runs of equal length become groups; per group
+// and channel the units' signed base links merge into at most two link rows
+// with coefficients +-1, and the distinct combinations (up to sign) become the
+// virtual rows, at most six.  Leaves grouped = 0 when a set does not fit.
 void make_groups(flr::FusedTdiSet &s) {
     s.grouped = 0;
+    s.num_vrows = 0;
     int ng = 0;
     for (int u = 0; u < s.num_units;) {
         int v = u;
@@ -119,18 +121,36 @@ void make_groups(flr::FusedTdiSet &s) {
         s.group_len[ng] = s.delay_len[u];
         s.group_start[ng] = u;
         for (int c = 0; c < 3; ++c) {
-            int terms = 0;
-            for (int q = 0; q < 2; ++q) {
-                s.group_row[ng][c][q] = 0;
-                s.group_sign[ng][c][q] = 0.f;
-            }
-            for (int slot = 0; slot < 6; ++slot) {
-                if (coef[c][slot] == 0.0) continue;
-                if (terms == 2 || (coef[c][slot] != 1.0 && coef[c][slot] != -1.0)) return;
-                s.group_row[ng][c][terms] = slot;
-                s.group_sign[ng][c][terms] = (float)coef[c][slot];
+            int slot[2] = {0, 0}, terms = 0;
+            float cf[2] = {0.f, 0.f};
+            for (int k = 0; k < 6; ++k) {
+                if (coef[c][k] == 0.0) continue;
+                if (terms == 2 || (coef[c][k] != 1.0 && coef[c][k] != -1.0)) return;
+                slot[terms] = k;
+                cf[terms] = (float)coef[c][k];
                 ++terms;
             }
+            s.group_vrow[ng][c] = 0;
+            s.group_vsign[ng][c] = 0.f;
+            if (terms == 0) continue;
+            // canonical combination: first coefficient +1, the sign kept apart
+            const float sg = cf[0];
+            const int b = (terms == 2) ? slot[1] : slot[0];
+            const float ca = 1.f, cb = (terms == 2) ? cf[1] * sg : 0.f;
+            int r = 0;
+            while (r < s.num_vrows && !(s.vrow_a[r] == slot[0] && s.vrow_b[r] == b &&
+                                        s.vrow_ca[r] == ca && s.vrow_cb[r] == cb))
+                ++r;
+            if (r == s.num_vrows) {
+                if (r == 6) return;
+                s.vrow_a[r] = slot[0];
+                s.vrow_b[r] = b;
+                s.vrow_ca[r] = ca;
+                s.vrow_cb[r] = cb;
+                ++s.num_vrows;
+            }
+            s.group_vrow[ng][c] = r;
+            s.group_vsign[ng][c] = sg;
         }
         ++ng;
         u = v;

@@ -475,13 +475,12 @@ __device__ __forceinline__ void store_channels(double *out, long n, long i, int 
 }
 
 // Grouped real interpolation: for each channel c the interpolation at one
-// delay (d, eps) of the row combination s0 y[r0] + s1 y[r1] (rows at shared
-// offsets off[c][*], signs sg[c][*] in {-1, 0, +1}); the weights are computed
-// once for the three channels.
-__device__ __forceinline__ void df_interp_group(const float2 *y, const int off[3][2],
-                                                const float sg[3][2], int d, df::f2 A,
-                                                df::f2 eps, const df::f2 *edf, int h,
-                                                df::f2 out[3]) {
+// delay (d, eps) of the virtual row at shared offset off[c], times sg[c]
+// (+-1; 0: the channel has no term here); the weights are computed once for
+// the three channels.
+__device__ __forceinline__ void df_interp_group(const float2 *y, const int off[3],
+                                                const float sg[3], int d, df::f2 A, df::f2 eps,
+                                                const df::f2 *edf, int h, df::f2 out[3]) {
     const DfWeights w = df_weights(A, eps);
     df::Acc acc[3];
 #pragma unroll
@@ -489,10 +488,8 @@ __device__ __forceinline__ void df_interp_group(const float2 *y, const int off[3
     auto tap = [&](df::f2 W, int k) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const float2 v0 = y[off[c][0] + k], v1 = y[off[c][1] + k];
-            const df::f2 z = df::add({sg[c][0] * v0.x, sg[c][0] * v0.y},
-                                     {sg[c][1] * v1.x, sg[c][1] * v1.y});
-            df::acc_fma(acc[c], W, z);
+            const float2 v = y[off[c] + k];
+            df::acc_fma(acc[c], W, {v.x, v.y});
         }
     };
     tap(df::mul_raw(w.A, w.ome), d + 1);
@@ -503,16 +500,21 @@ __device__ __forceinline__ void df_interp_group(const float2 *y, const int off[3
         tap(df::mul_raw(cE, df::rcp(df::add_big_float((float)j, w.ome))), d - j);
     }
 #pragma unroll
-    for (int c = 0; c < 3; ++c) out[c] = df::acc_value(acc[c]);
+    for (int c = 0; c < 3; ++c) {
+        const df::f2 v = df::acc_value(acc[c]);
+        out[c] = (sg[c] == 0.f) ? df::f2{0.f, 0.f} : df::f2{sg[c] * v.hi, sg[c] * v.lo};
+    }
 }
 
 // -------------------------------------------------------------- the kernel ----
 
-// Register budgets are the compiler's own choice: pinning the grouped
-// instance to three blocks per SM (80 registers) measured 2.5 % slower than
-// its unbounded 128 registers at two blocks per SM.
+// Register budgets: the grouped mixed instance is sized for three blocks per
+// SM (80 registers), which measured 3 % faster than the compiler's 96
+// registers at two; the others keep the compiler's choice (a minimum of 0
+// blocks leaves it unspecified).
 template <bool kMixed, bool kDiag, bool kGrouped>
-__global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
+__global__ void __launch_bounds__(kThreads, (kGrouped && !kDiag) ? 3 : 0)
+    fused_kernel(const FusedArgs a) {
     static_assert(kMixed || !kGrouped, "the grouped form is a mixed-arithmetic form");
     extern __shared__ __align__(128) unsigned char smem[];
     const Layout lay = layout(kMixed, a.win_max, a.y_max);
@@ -816,6 +818,27 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
         }
         __syncthreads();
 
+        // 4b. grouped form: the link rows become the set's virtual rows, in
+        // place (each thread reads a sample's six rows before writing them)
+        if (kGrouped) {
+            for (int jj = tid; jj < Y; jj += kThreads) {
+                df::f2 z[6];
+#pragma unroll
+                for (int r = 0; r < 6; ++r) {
+                    if (r < set->num_vrows) {
+                        const float ca = set->vrow_ca[r], cb = set->vrow_cb[r];
+                        const float2 va = y32[set->vrow_a[r] * a.y_max + jj];
+                        const float2 vb = y32[set->vrow_b[r] * a.y_max + jj];
+                        z[r] = df::add({ca * va.x, ca * va.y}, {cb * vb.x, cb * vb.y});
+                    }
+                }
+#pragma unroll
+                for (int r = 0; r < 6; ++r)
+                    if (r < set->num_vrows) y32[r * a.y_max + jj] = make_float2(z[r].hi, z[r].lo);
+            }
+            __syncthreads();
+        }
+
         // 5. TDI for the output samples [o0, o1)
         const double inv_scale = 1.0 / scale;
         if (kGrouped) {
@@ -842,19 +865,17 @@ __global__ void __launch_bounds__(kThreads) fused_kernel(const FusedArgs a) {
                         raise_status(a.orb.status, kStatusTap);
 #pragma unroll
                         for (int c = 0; c < 3; ++c)
-                            if (set->group_sign[g][c][0] != 0.f || set->group_sign[g][c][1] != 0.f)
+                            if (set->group_vsign[g][c] != 0.f)
                                 accdf[c] = {__int_as_float(0x7fc00000), 0.f};
                         continue;
                     }
-                    int off[3][2];
-                    float sg[3][2];
+                    int off[3];
+                    float sg[3];
 #pragma unroll
-                    for (int c = 0; c < 3; ++c)
-#pragma unroll
-                        for (int q = 0; q < 2; ++q) {
-                            off[c][q] = set->group_row[g][c][q] * a.y_max;
-                            sg[c][q] = set->group_sign[g][c][q];
-                        }
+                    for (int c = 0; c < 3; ++c) {
+                        off[c] = set->group_vrow[g][c] * a.y_max;
+                        sg[c] = set->group_vsign[g][c];
+                    }
                     const df::f2 A_df = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_df);
                     df::f2 val[3];
                     df_interp_group(y32, off, sg, (int)(d - ya), A_df, e_df, edf, h, val);

@@ -53,19 +53,23 @@ struct FusedTdiSet {
     // Grouped form, for mixed arithmetic on equal-arm orbits, where every L(t)
     // is the same value and units with delay lists of equal length have
     // bitwise-equal delays.  Group g holds the units [group_start[g],
-    // group_start[g + 1]) (lists of length group_len[g], ascending) and adds to
-    // channel c the interpolation, at that one delay, of the signed link-row
-    // combination group_sign[g][c][0] y[group_row[g][c][0]] +
-    // group_sign[g][c][1] y[group_row[g][c][1]] (a sign of 0 marks an unused
-    // term): by linearity the sum of the units' interpolations.  grouped = 0
-    // when the set does not take this form (more than two links or a
-    // coefficient other than +-1 in some group and channel).
+    // group_start[g + 1]) (lists of length group_len[g], ascending); by
+    // linearity their sum on channel c is the interpolation, at that one
+    // delay, of group_vsign[g][c] (+-1, 0: none) times the virtual row
+    // group_vrow[g][c].  Virtual row r = vrow_ca[r] y[vrow_a[r]] +
+    // vrow_cb[r] y[vrow_b[r]] (coefficients +-1 or 0) replaces the link rows
+    // in shared memory once per tile.  grouped = 0 when the set does not take
+    // this form (a group and channel combining more than two links or with a
+    // coefficient other than +-1, or more than six distinct combinations).
     int grouped;
     int num_groups;
+    int num_vrows;
     int group_len[kFusedMaxGroups];
     int group_start[kFusedMaxGroups + 1];
-    int group_row[kFusedMaxGroups][3][2];
-    float group_sign[kFusedMaxGroups][3][2];
+    int group_vrow[kFusedMaxGroups][3];
+    float group_vsign[kFusedMaxGroups][3];
+    int vrow_a[6], vrow_b[6];
+    float vrow_ca[6], vrow_cb[6];
 };
 
 enum FusedChan { kChanXYZ = 0, kChanAET = 1, kChanAE = 2 };
