@@ -687,7 +687,75 @@ __global__ void __launch_bounds__(kThreads, (kGrouped && !kDiag) ? 3 : 0)
         // iteration, the receiver's position, index split and interpolation
         // shared by its two links (the same values the per-link form computes
         // twice).  Otherwise one (link, sample) per thread iteration.
-        if (kMixed && a.rx_shared) {
+        if (kGrouped && a.trio) {
+            // Equal arms (the grouped form implies them): every link leaving a
+            // spacecraft has the same t_em, so a sample needs three receiver
+            // and three emitter interpolations.  Three lanes per sample (ten
+            // samples per warp, lanes 30-31 idle): lane r computes spacecraft
+            // r + 1's receiver and emitter sides and takes the emitter sides of
+            // its two links from the other lanes of its trio.
+            const int lane = tid & 31, sub = lane / 3, r = lane - 3 * sub;
+            const int rr = (r < 3) ? r : 0;
+            for (int base = (tid >> 5) * 10; base < Y; base += 10 * (kThreads / 32)) {
+                const int jj = base + sub;
+                const bool act = (sub < 10) && (jj < Y);
+                const long j = ya + jj;
+                const bool live = act && j >= yfirst && j < ylast;
+                const double t = t0 + (double)j * a.dt;
+                ReceiverSide rs{};
+                EmitterSide es{};
+                df::f2 re_r = {0.f, 0.f}, im_r = {0.f, 0.f}, re_e = {0.f, 0.f}, im_e = {0.f, 0.f};
+                bool ok_r = false, ok_e = false;
+                if (live) {
+                    rs = receiver_mixed(a.orb, a.inv_orbit_dt, rr + 1, t, t0, a.fs, k);
+                    ok_r = df_interp_c128_any(
+                        hdf, dh, wlo, W, src.h, scale, n, rs.d_rec,
+                        prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, rs.e_rec), rs.e_rec, edf,
+                        h, re_r, im_r);
+                    es = emitter_mixed(a.orb, a.inv_orbit_dt, a.tx_slot[rr], rs.w, t, t0, a.fs, k);
+                    ok_e = df_interp_c128_any(
+                        hdf, dh, wlo, W, src.h, scale, n, es.d_em,
+                        prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, es.e_em), es.e_em, edf,
+                        h, re_e, im_e);
+                }
+                const bool own = live && (j >= o0 && j < o1);  // diagnostics
+                for (int q = 0; q < 2; ++q) {
+                    const int slot = a.rx_slot[rr][q];
+                    const int from = min(3 * sub + a.orb.sc_e[slot] - 1, 31);
+                    const unsigned full = 0xffffffffu;
+                    const df::f2 xre = {__shfl_sync(full, re_e.hi, from),
+                                        __shfl_sync(full, re_e.lo, from)};
+                    const df::f2 xim = {__shfl_sync(full, im_e.hi, from),
+                                        __shfl_sync(full, im_e.lo, from)};
+                    const bool xok = __shfl_sync(full, (int)ok_e, from) != 0;
+                    double x_em[3];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) x_em[c] = __shfl_sync(full, es.x_em[c], from);
+                    const int d_em = __shfl_sync(full, es.d_em, from);
+                    if (!act) continue;
+                    if (!live) {  // the reference's y_gw is zero there
+                        y32[slot * a.y_max + jj] = make_float2(0.f, 0.f);
+                        continue;
+                    }
+                    if (kDiag && own && src.d_rec_out) {
+                        src.d_rec_out[(long)slot * n + j] = rs.d_rec;
+                        src.d_em_out[(long)slot * n + j] = d_em;
+                    }
+                    if (!ok_r || !xok) {
+                        raise_status(a.orb.status, kStatusTap);
+                        y32[slot * a.y_max + jj] = make_float2(__int_as_float(0x7fc00000), 0.f);
+                        continue;
+                    }
+                    const DfProjection pr = df_projection(rs.x_rec, x_em, kdf, udf, vdf);
+                    const df::f2 dre = df::sub(xre, re_r), dim = df::sub(xim, im_r);
+                    df::f2 yv = df::add(df::mul(dre, pr.xi_p), df::mul(dim, pr.xi_c));
+                    yv = df::mul(yv, pr.pre);
+                    y32[slot * a.y_max + jj] = make_float2(yv.hi, yv.lo);
+                    if (kDiag && own && src.y_out)
+                        src.y_out[(long)slot * n + j] = df::to_double(yv) / scale;
+                }
+            }
+        } else if (kMixed && a.rx_shared) {
             for (int it = tid; it < 3 * Y; it += kThreads) {
                 const int r = it / Y;
                 const int jj = it - r * Y;

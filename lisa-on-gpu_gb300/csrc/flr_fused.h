@@ -101,6 +101,10 @@ struct FusedArgs {
     int rx_shared;
     int rx_sc[3];
     int rx_slot[3][2];
+    // tx_slot[r]: a link spacecraft r + 1 emits on (trio = 1 when all three
+    // emit; with equal arms all links leaving a spacecraft share t_em)
+    int trio;
+    int tx_slot[3];
 };
 
 // Galactic-binary parameters of one source (on-device waveform generation).
