@@ -224,6 +224,15 @@ typedef struct {
     int *d_rec_out;
     int *d_em_out;
     int *d_tdi_out;
+    /* Optional inner products (both NULL = off): data [3][n] float64 device
+     * channels in the layout of out; inner [6] float64 device receives
+     * <h_c|d_c> for c = 0, 1, 2 then <h_c|h_c>, summed over the computed samples
+     * [tdi_start, n - tdi_start) in a fixed order (deterministic).  With inner
+     * set, out may be NULL: the channels are then never written to memory.
+     * Not available through batch graphs.  (The reference's consumer,
+     * utils/utility.py:16-82, forms such products from the stored channels.) */
+    const double *data;
+    double *inner;
 } flr_batch_source;
 
 typedef struct flr_batch_plan flr_batch_plan;

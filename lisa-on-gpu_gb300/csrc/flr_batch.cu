@@ -47,6 +47,8 @@ struct flr_batch_plan {
     cudaEvent_t stage_free;    // recorded after the staging copies of the last run
     bool stage_pending;
     cudaEvent_t done;          // recorded after the kernels of the last run
+    double *d_partial;         // per-tile partial inner products (runs that ask for them)
+    size_t cap_partial;
     bool done_pending;
 };
 
@@ -97,6 +99,7 @@ void release(flr_batch_plan *p) {
     if (!p) return;
     if (p->d_tables) cudaFree(p->d_tables);
     if (p->d_stage) cudaFree(p->d_stage);
+    if (p->d_partial) cudaFree(p->d_partial);
     if (p->h_stage) cudaFreeHost(p->h_stage);
     if (p->stage_free) cudaEventDestroy(p->stage_free);
     if (p->done) cudaEventDestroy(p->done);
@@ -178,30 +181,36 @@ StageLayout stage_layout(int cap, bool waveforms) {
 
 // Check the sources and write their staging image for `cap` descriptors
 // (entries num_sources..cap-1 are empty: no tiles, no chunks).  `diag` is set
-// when a source asks for diagnostics.
+// when a source asks for diagnostics, `inner` when one asks for inner
+// products; `total_tiles` receives the run's work items.
 int fill_stage(const flr_batch_plan *plan, const flr_batch_source *sources, int num_sources,
                const flr_gb_params *gb, int cap, const StageLayout &lay, unsigned char *hs,
-               bool *diag) {
+               bool *diag, bool *inner, long *total_tiles) {
     const int tile = plan->base.tile;
     flr::FusedSource *srcs = reinterpret_cast<flr::FusedSource *>(hs);
     long *tile_start = reinterpret_cast<long *>(hs + lay.tiles);
     long *chunk_start = reinterpret_cast<long *>(hs + lay.chunks);
     long tiles = 0, chunks = 0;
     *diag = false;
+    *inner = false;
     for (int i = 0; i < num_sources; ++i) {
         const flr_batch_source &s = sources[i];
-        if (!s.h || !s.out || s.n < 2 || s.projections_start < 0 ||
+        if (!s.h || (!s.out && !s.inner) || s.n < 2 || s.projections_start < 0 ||
             s.tdi_start < s.projections_start || 2LL * s.tdi_start >= s.n ||
             s.n > (1LL << 31) - 1 || s.tdi_set < 0 || s.tdi_set >= plan->num_sets)
             return fail(FLR_E_INVALID_ARGUMENT,
                         "source " + std::to_string(i) +
-                            ": need h, out, 0 <= projections_start <= tdi_start < n/2, "
+                            ": need h, out (or inner), 0 <= projections_start <= tdi_start "
+                            "< n/2, "
                             "n < 2^31 and a valid tdi_set");
         if (reinterpret_cast<uintptr_t>(s.h) % 16 != 0)
             return fail(FLR_E_INVALID_ARGUMENT, "source " + std::to_string(i) +
                                                     ": h (complex128) must be 16-byte aligned");
         if ((s.d_rec_out == nullptr) != (s.d_em_out == nullptr))
             return fail(FLR_E_INVALID_ARGUMENT, "d_rec_out and d_em_out go together");
+        if ((s.data == nullptr) != (s.inner == nullptr))
+            return fail(FLR_E_INVALID_ARGUMENT, "source " + std::to_string(i) +
+                                                    ": data and inner go together");
         flr::FusedSource d{};
         d.h = static_cast<const double2 *>(s.h);
         d.out = s.out;
@@ -219,7 +228,10 @@ int fill_stage(const flr_batch_plan *plan, const flr_batch_source *sources, int 
         d.d_rec_out = s.d_rec_out;
         d.d_em_out = s.d_em_out;
         d.d_tdi_out = s.d_tdi_out;
+        d.data = s.data;
+        d.inner = s.inner;
         *diag = *diag || s.y_out || s.d_rec_out || s.d_tdi_out;
+        *inner = *inner || s.inner;
         std::memcpy(srcs + i, &d, sizeof(d));
         tile_start[i] = tiles;
         tiles += (long)((s.n - 2LL * s.tdi_start + tile - 1) / tile);
@@ -231,6 +243,7 @@ int fill_stage(const flr_batch_plan *plan, const flr_batch_source *sources, int 
         }
     }
     if (tiles > 0x7fffffffL) return fail(FLR_E_INVALID_ARGUMENT, "too many tiles");
+    *total_tiles = tiles;
     if (cap > num_sources) {
         std::memset(srcs + num_sources, 0, sizeof(flr::FusedSource) * (size_t)(cap - num_sources));
         if (gb)
@@ -247,7 +260,7 @@ int fill_stage(const flr_batch_plan *plan, const flr_batch_source *sources, int 
 // The copy of a staging image to `d_stage` and the kernels that read it.
 cudaError_t enqueue(const flr_batch_plan *plan, const unsigned char *h_stage,
                     unsigned char *d_stage, const StageLayout &lay, int cap, bool waveforms,
-                    bool diag, int chan, cudaEvent_t copied, cudaStream_t st) {
+                    bool diag, double *partial, int chan, cudaEvent_t copied, cudaStream_t st) {
     cudaError_t err = cudaMemcpyAsync(d_stage, h_stage, lay.bytes, cudaMemcpyHostToDevice, st);
     if (err == cudaSuccess && copied) err = cudaEventRecord(copied, st);
     if (err != cudaSuccess) return err;
@@ -264,7 +277,11 @@ cudaError_t enqueue(const flr_batch_plan *plan, const unsigned char *h_stage,
     a.tile_start = reinterpret_cast<const long *>(d_stage + lay.tiles);
     a.num_sources = cap;
     a.chan = chan;
-    return flr::launch_fused(plan->mixed, plan->grouped, diag, a, plan->grid_max, plan->smem, st);
+    a.partial = partial;
+    err = flr::launch_fused(plan->mixed, plan->grouped, diag, partial != nullptr, a, plan->grid_max,
+                            plan->smem, st);
+    if (err == cudaSuccess && partial) err = flr::launch_inner_reduce(a, st);
+    return err;
 }
 
 void release_graph(flr_batch_graph *g) {
@@ -562,9 +579,13 @@ static int batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int 
         if (err != cudaSuccess) return cuda_fail(err, "allocating the staging buffer");
         plan->cap_stage = lay.bytes * 2;
     }
-    bool diag = false;
-    rc = fill_stage(plan, sources, num_sources, gb, num_sources, lay, plan->h_stage, &diag);
+    bool diag = false, inner = false;
+    long tiles = 0;
+    rc = fill_stage(plan, sources, num_sources, gb, num_sources, lay, plan->h_stage, &diag, &inner,
+                    &tiles);
     if (rc) return rc;
+    if (diag && inner)
+        return fail(FLR_E_INVALID_ARGUMENT, "diagnostics and inner products need separate runs");
     // the device staging buffer is reused: a previous run on another stream
     // must have finished reading it
     if (plan->done_pending) {
@@ -583,8 +604,21 @@ static int batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int 
         if (err != cudaSuccess) return cuda_fail(err, "allocating the staging buffer");
         plan->cap_device = lay.bytes * 2;
     }
-    err = enqueue(plan, plan->h_stage, plan->d_stage, lay, num_sources, gb != nullptr, diag, chan,
-                  plan->stage_free, st);
+    const size_t partial_bytes = sizeof(double) * 6 * (size_t)tiles;
+    if (inner && partial_bytes > plan->cap_partial) {
+        if (plan->d_partial) {  // an earlier run may still read it
+            err = cudaDeviceSynchronize();
+            if (err == cudaSuccess) err = cudaFree(plan->d_partial);
+            if (err != cudaSuccess) return cuda_fail(err, "releasing the inner-product buffer");
+        }
+        plan->d_partial = nullptr;
+        plan->cap_partial = 0;
+        err = cudaMalloc(&plan->d_partial, partial_bytes + partial_bytes / 2);
+        if (err != cudaSuccess) return cuda_fail(err, "allocating the inner-product buffer");
+        plan->cap_partial = partial_bytes + partial_bytes / 2;
+    }
+    err = enqueue(plan, plan->h_stage, plan->d_stage, lay, num_sources, gb != nullptr, diag,
+                  inner ? plan->d_partial : nullptr, chan, plan->stage_free, st);
     plan->stage_pending = true;
     if (err != cudaSuccess) return cuda_fail(err, "launching the batch");
     err = cudaEventRecord(plan->done, st);
@@ -639,7 +673,7 @@ int flr_batch_graph_create(flr_batch_plan *plan, int max_sources, int flags, int
         err = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
         if (err != cudaSuccess) break;
         const cudaError_t e_enq = enqueue(plan, g->h_stage[b], g->d_stage, lay, g->cap,
-                                          g->waveforms, g->diag, chan, nullptr, cs);
+                                          g->waveforms, g->diag, nullptr, chan, nullptr, cs);
         cudaGraph_t graph = nullptr;
         const cudaError_t e_end = cudaStreamEndCapture(cs, &graph);
         err = (e_enq != cudaSuccess) ? e_enq : e_end;
@@ -676,10 +710,14 @@ int flr_batch_graph_launch(flr_batch_graph *g, const flr_batch_source *sources,
         g->pending[b] = false;
     }
     const StageLayout lay = stage_layout(g->cap, g->waveforms);
-    bool diag = false;
+    bool diag = false, inner = false;
+    long tiles = 0;
     rc = fill_stage(g->plan, sources, num_sources, g->waveforms ? params : nullptr, g->cap, lay,
-                    g->h_stage[b], &diag);
+                    g->h_stage[b], &diag, &inner, &tiles);
     if (rc) return rc;
+    if (inner)
+        return fail(FLR_E_INVALID_ARGUMENT,
+                    "inner products are not available through batch graphs: use flr_batch_run");
     if (diag && !g->diag)
         return fail(FLR_E_INVALID_ARGUMENT,
                     "diagnostics need a graph created with FLR_GRAPH_DIAGNOSTICS");

@@ -474,6 +474,28 @@ __device__ __forceinline__ void store_channels(double *out, long n, long i, int 
     }
 }
 
+// Inner-product form of store_channels: the same channel values, added to
+// lk[c] += value_c * data_c[i] and lk[3 + c] += value_c^2.
+__device__ __forceinline__ void add_inner(double lk[6], const double *data, long n, long i,
+                                          int chan, double X, double Yc, double Z) {
+    double c0, c1, c2;
+    if (chan == kChanXYZ) {
+        c0 = X;
+        c1 = Yc;
+        c2 = Z;
+    } else {
+        c0 = (Z - X) / 1.4142135623730951;
+        c1 = (X - 2.0 * Yc + Z) / 2.449489742783178;
+        c2 = (chan == kChanAET) ? (X + Yc + Z) / 1.7320508075688772 : 0.0;
+    }
+    lk[0] += c0 * data[i];
+    lk[1] += c1 * data[n + i];
+    lk[2] += c2 * data[2 * n + i];
+    lk[3] += c0 * c0;
+    lk[4] += c1 * c1;
+    lk[5] += c2 * c2;
+}
+
 // Grouped real interpolation: for each channel c the interpolation at one
 // delay (d, eps) of the virtual row at shared offset off[c], times sg[c]
 // (+-1; 0: the channel has no term here); the weights are computed once for
@@ -512,10 +534,13 @@ __device__ __forceinline__ void df_interp_group(const float2 *y, const int off[3
 // SM (80 registers), which measured 3 % faster than the compiler's 96
 // registers at two; the others keep the compiler's choice (a minimum of 0
 // blocks leaves it unspecified).
-template <bool kMixed, bool kDiag, bool kGrouped>
+// kInner: the instance that forms per-tile inner products with FusedSource
+// data (FusedArgs::partial) and writes the channels only where out is set.
+template <bool kMixed, bool kDiag, bool kGrouped, bool kInner>
 __global__ void __launch_bounds__(kThreads, (kGrouped && !kDiag) ? 3 : 0)
     fused_kernel(const FusedArgs a) {
     static_assert(kMixed || !kGrouped, "the grouped form is a mixed-arithmetic form");
+    static_assert(!(kDiag && kInner), "diagnostics and inner products are separate instances");
     extern __shared__ __align__(128) unsigned char smem[];
     const Layout lay = layout(kMixed, a.win_max, a.y_max);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
@@ -582,7 +607,7 @@ __global__ void __launch_bounds__(kThreads, (kGrouped && !kDiag) ? 3 : 0)
         const long o1 = min(o0 + (long)a.tile, n - ts);
         // the first and last tiles also write the zeros of the edge zones
         // [0, ts) and [n - ts, n), so outputs need no clearing beforehand
-        if (tile_idx == 0 || o1 == n - ts) {
+        if ((tile_idx == 0 || o1 == n - ts) && (!kInner || src.out)) {
             const long e0 = (tile_idx == 0) ? 0 : n - ts;
             for (int c = 0; c < 3; ++c)
                 for (long i = e0 + tid; i < e0 + ts; i += kThreads) src.out[c * n + i] = 0.0;
@@ -909,6 +934,7 @@ __global__ void __launch_bounds__(kThreads, (kGrouped && !kDiag) ? 3 : 0)
 
         // 5. TDI for the output samples [o0, o1)
         const double inv_scale = 1.0 / scale;
+        double lk[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // inner products (kInner)
         if (kGrouped) {
             for (long i = o0 + tid; i < o1; i += kThreads) {
                 const double t = t0 + (double)i * a.dt;
@@ -953,7 +979,8 @@ __global__ void __launch_bounds__(kThreads, (kGrouped && !kDiag) ? 3 : 0)
                 const double X = df::to_double(accdf[0]) * inv_scale;
                 const double Yc = df::to_double(accdf[1]) * inv_scale;
                 const double Z = df::to_double(accdf[2]) * inv_scale;
-                store_channels(src.out, n, i, a.chan, X, Yc, Z);
+                if (!kInner || src.out) store_channels(src.out, n, i, a.chan, X, Yc, Z);
+                if (kInner && src.data) add_inner(lk, src.data, n, i, a.chan, X, Yc, Z);
             }
         } else {
             for (long i = o0 + tid; i < o1; i += kThreads) {
@@ -1038,11 +1065,44 @@ __global__ void __launch_bounds__(kThreads, (kGrouped && !kDiag) ? 3 : 0)
                     Yc = acc64[1];
                     Z = acc64[2];
                 }
-                store_channels(src.out, n, i, a.chan, X, Yc, Z);
+                if (!kInner || src.out) store_channels(src.out, n, i, a.chan, X, Yc, Z);
+                if (kInner && src.data) add_inner(lk, src.data, n, i, a.chan, X, Yc, Z);
+            }
+        }
+        if (kInner) {
+            // the tile's six sums, reduced in a fixed order: lanes by xor
+            // shuffles, then the warps in index order (deterministic)
+#pragma unroll
+            for (int q = 0; q < 6; ++q)
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1)
+                    lk[q] += __shfl_xor_sync(0xffffffffu, lk[q], off);
+            __syncthreads();  // the link rows are read no more: their space takes the warp sums
+            double *red = reinterpret_cast<double *>(smem + lay.y);
+            if ((tid & 31) == 0)
+#pragma unroll
+                for (int q = 0; q < 6; ++q) red[(tid >> 5) * 6 + q] = lk[q];
+            __syncthreads();
+            if (tid < 6) {
+                double sum = 0.0;
+                for (int w = 0; w < kThreads / 32; ++w) sum += red[w * 6 + tid];
+                a.partial[wi * 6 + tid] = sum;
             }
         }
         __syncthreads();
     }
+}
+
+// One thread per (source, quantity): the source's per-tile partial sums added
+// in tile order.
+__global__ void inner_reduce_kernel(const FusedSource *src, const long *tile_start,
+                                    int num_sources, const double *partial) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = (int)(idx / 6), q = (int)(idx - 6L * (idx / 6));
+    if (s >= num_sources || src[s].inner == nullptr) return;
+    double sum = 0.0;
+    for (long w = tile_start[s]; w < tile_start[s + 1]; ++w) sum += partial[w * 6 + q];
+    src[s].inner[q] = sum;
 }
 
 }  // namespace
@@ -1051,34 +1111,49 @@ size_t fused_smem_bytes(bool mixed, int win_max, int y_max) {
     return layout(mixed, win_max, y_max).total;
 }
 
-static const void *fused_fn(bool mixed, bool grouped, bool diag) {
+static const void *fused_fn(bool mixed, bool grouped, bool diag, bool inner) {
+    if (inner) {
+        if (mixed && grouped)
+            return reinterpret_cast<const void *>(fused_kernel<true, false, true, true>);
+        if (mixed) return reinterpret_cast<const void *>(fused_kernel<true, false, false, true>);
+        return reinterpret_cast<const void *>(fused_kernel<false, false, false, true>);
+    }
     if (mixed && grouped)
-        return diag ? reinterpret_cast<const void *>(fused_kernel<true, true, true>)
-                    : reinterpret_cast<const void *>(fused_kernel<true, false, true>);
+        return diag ? reinterpret_cast<const void *>(fused_kernel<true, true, true, false>)
+                    : reinterpret_cast<const void *>(fused_kernel<true, false, true, false>);
     if (mixed)
-        return diag ? reinterpret_cast<const void *>(fused_kernel<true, true, false>)
-                    : reinterpret_cast<const void *>(fused_kernel<true, false, false>);
-    return diag ? reinterpret_cast<const void *>(fused_kernel<false, true, false>)
-                : reinterpret_cast<const void *>(fused_kernel<false, false, false>);
+        return diag ? reinterpret_cast<const void *>(fused_kernel<true, true, false, false>)
+                    : reinterpret_cast<const void *>(fused_kernel<true, false, false, false>);
+    return diag ? reinterpret_cast<const void *>(fused_kernel<false, true, false, false>)
+                : reinterpret_cast<const void *>(fused_kernel<false, false, false, false>);
 }
 
 cudaError_t fused_configure(bool mixed, bool grouped, size_t smem_bytes, int *blocks_per_sm) {
-    for (bool diag : {true, false}) {
-        cudaError_t err = cudaFuncSetAttribute(fused_fn(mixed, grouped, diag),
+    for (int v = 0; v < 3; ++v) {  // plain, diagnostics, inner products
+        cudaError_t err = cudaFuncSetAttribute(fused_fn(mixed, grouped, v == 1, v == 2),
                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)smem_bytes);
         if (err != cudaSuccess) return err;
     }
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        blocks_per_sm, fused_fn(mixed, grouped, false), kThreads, smem_bytes);
+        blocks_per_sm, fused_fn(mixed, grouped, false, false), kThreads, smem_bytes);
 }
 
-cudaError_t launch_fused(bool mixed, bool grouped, bool diag, const FusedArgs &a, int grid,
-                         size_t smem_bytes, cudaStream_t stream) {
+cudaError_t launch_fused(bool mixed, bool grouped, bool diag, bool inner, const FusedArgs &a,
+                         int grid, size_t smem_bytes, cudaStream_t stream) {
     if (a.num_sources <= 0) return cudaSuccess;
+    if (diag && inner) return cudaErrorInvalidValue;
     void *args[] = {const_cast<FusedArgs *>(&a)};
-    return cudaLaunchKernel(fused_fn(mixed, grouped, diag), dim3(grid), dim3(kThreads), args,
-                            smem_bytes, stream);
+    return cudaLaunchKernel(fused_fn(mixed, grouped, diag, inner), dim3(grid), dim3(kThreads),
+                            args, smem_bytes, stream);
+}
+
+cudaError_t launch_inner_reduce(const FusedArgs &a, cudaStream_t stream) {
+    if (a.num_sources <= 0) return cudaSuccess;
+    const long threads = 6L * a.num_sources;
+    inner_reduce_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, stream>>>(
+        a.sources, a.tile_start, a.num_sources, a.partial);
+    return cudaGetLastError();
 }
 
 }  // namespace flr

@@ -29,6 +29,10 @@ struct FusedSource {
     int *d_rec_out;     // [6][n] receiver integer delays
     int *d_em_out;      // [6][n] emitter integer delays
     int *d_tdi_out;     // [num_units][n] TDI integer delays, in the caller's unit order
+    // optional inner products (NULL = off): data [3][n]; inner [6] =
+    // <h_c|d_c> (c = 0..2), then <h_c|h_c>, over [ts, n - ts)
+    const double *data;
+    double *inner;
 };
 
 // TDI unit tables with link numbers already mapped to link slots.
@@ -84,6 +88,9 @@ struct FusedArgs {
     // device, so a captured launch can run batches of any lengths.
     const long *tile_start;
     int num_sources;
+    // per work item: the six partial inner products of its tile (inner-product
+    // runs only; reduced per source by launch_inner_reduce)
+    double *partial;
     const FusedTdiSet *sets;
     int num_sets;
     const float4 *a_tab;       // per A-table knot: (A hi, A lo, dA hi, dA lo), dA = A[k+1]-A[k]
@@ -122,9 +129,13 @@ cudaError_t launch_gb_waveforms(const FusedSource *src, const GbParams *par,
 size_t fused_smem_bytes(bool mixed, int win_max, int y_max);
 // grouped: the mixed instance for sets in grouped form (every set of the plan).
 cudaError_t fused_configure(bool mixed, bool grouped, size_t smem_bytes, int *blocks_per_sm);
-// diag: the instance that writes the FusedSource diagnostics (more registers).
-cudaError_t launch_fused(bool mixed, bool grouped, bool diag, const FusedArgs &a, int grid,
-                         size_t smem_bytes,
+// Sum each source's per-tile partial inner products, tiles in order, into
+// its inner[6] (sources without inner are skipped).
+cudaError_t launch_inner_reduce(const FusedArgs &a, cudaStream_t stream);
+// diag: the instance that writes the FusedSource diagnostics (more registers);
+// inner: the instance that forms inner products (FusedArgs::partial set).
+cudaError_t launch_fused(bool mixed, bool grouped, bool diag, bool inner, const FusedArgs &a,
+                         int grid, size_t smem_bytes,
                          cudaStream_t stream);
 
 }  // namespace flr

@@ -72,7 +72,9 @@ class _Source(ctypes.Structure):
                 ("y_out", ctypes.c_void_p),
                 ("d_rec_out", ctypes.c_void_p),
                 ("d_em_out", ctypes.c_void_p),
-                ("d_tdi_out", ctypes.c_void_p)]
+                ("d_tdi_out", ctypes.c_void_p),
+                ("data", ctypes.c_void_p),
+                ("inner", ctypes.c_void_p)]
 
 
 def _combinations(spec):
@@ -274,8 +276,68 @@ class BatchedResponseTDI:
                          self._bucket(ns, True, False) if use_graph else None)
         return outs, hs
 
+    def inner_products(self, h: Sequence, lam, beta, data: Sequence, t0=0.0, tdi_set=0,
+                       stream=None, write_out: bool = False):
+        """Channel inner products of each source's response with data, formed
+        inside the kernel: the channels need not be written to memory.
+
+        Args:
+            h, lam, beta, t0, tdi_set: as for __call__.
+            data: per source a (3, n) float64 CUDA tensor in the layout of the
+                output channels (X, Y, Z or A, E, T / A, E).
+            write_out: also return the channels (else they are never stored).
+        Returns:
+            (ns, 2, 3) float64 tensor: [i, 0, c] = <h_c|d_c>, [i, 1, c] =
+            <h_c|h_c>, sums over the computed samples [tdi_start, n - tdi_start)
+            in a fixed order (run to run identical); with write_out, (inner,
+            outs).  The white-noise log-likelihood follows as
+            -0.5 sum_c (<d|d> - 2 <h|d> + <h|h>) / sigma_c^2.
+        """
+        dev = self.device
+        hs = [_as_device(x, dev, torch.complex128) for x in h]
+        lengths = [len(x) for x in hs]
+        ds = self._check_data(data, lengths)
+        inner = torch.empty((len(hs), 6), dtype=torch.float64, device=dev)
+        outs = self._run(hs, None, lengths, lam, beta, t0, tdi_set, None, stream, False, None,
+                         data=ds, inner=inner, write_out=write_out)
+        inner = inner.view(len(hs), 2, 3)
+        return (inner, outs) if write_out else inner
+
+    def inner_products_gb(self, params, lengths, lam, beta, data: Sequence, t0=0.0, tdi_set=0,
+                          h=None, stream=None):
+        """inner_products() of galactic binaries whose waveforms are generated
+        on the device (run_gb's parameters); the channels are not stored.
+        Returns ((ns, 2, 3) inner products, waveforms)."""
+        params = np.asarray(params, dtype=np.float64).reshape(-1, 6)
+        ns = len(params)
+        lengths = [int(n) for n in np.broadcast_to(np.asarray(lengths, dtype=np.int64), (ns,))]
+        dev = self.device
+        hs = list(h) if h is not None else [
+            torch.empty(n, dtype=torch.complex128, device=dev) for n in lengths]
+        for i, n in enumerate(lengths):
+            if hs[i].numel() != n or hs[i].dtype != torch.complex128 or not hs[i].is_cuda:
+                raise ValueError(f"h[{i}] must be a complex128 CUDA buffer of {n} samples")
+        ds = self._check_data(data, lengths)
+        inner = torch.empty((ns, 6), dtype=torch.float64, device=dev)
+        self._run(hs, params, lengths, lam, beta, t0, tdi_set, None, stream, False, None,
+                  data=ds, inner=inner, write_out=False)
+        return inner.view(ns, 2, 3), hs
+
+    def _check_data(self, data, lengths):
+        ds = list(data)
+        if len(ds) != len(lengths):
+            raise ValueError("need one data array per source")
+        for i, (x, n) in enumerate(zip(ds, lengths)):
+            if (not isinstance(x, torch.Tensor) or tuple(x.shape) != (3, n)
+                    or x.dtype != torch.float64 or not x.is_cuda or not x.is_contiguous()
+                    or x.device != self.device):
+                raise ValueError(f"data[{i}] must be a contiguous (3, {n}) float64 tensor on "
+                                 f"{self.device}")
+        return ds
+
     # -- internals ----------------------------------------------------------------
-    def _run(self, hs, params, lengths, lam, beta, t0, tdi_set, out, stream, diagnostics, graph):
+    def _run(self, hs, params, lengths, lam, beta, t0, tdi_set, out, stream, diagnostics, graph,
+             data=None, inner=None, write_out=True):
         ns = len(hs)
         dev = self.device
         lam = np.broadcast_to(np.asarray(lam, dtype=np.float64), (ns,))
@@ -291,11 +353,17 @@ class BatchedResponseTDI:
                 if (tuple(o.shape) != (3, n) or o.dtype != torch.float64 or not o.is_cuda
                         or not o.is_contiguous()):
                     raise ValueError(f"out[{i}] must be a contiguous (3, {n}) float64 CUDA tensor")
-        else:
+        elif write_out:
             outs = [torch.empty((3, n), dtype=torch.float64, device=dev) for n in lengths]
+        else:
+            outs = None
         srcs = np.zeros(ns, dtype=SOURCE_DTYPE)
         srcs["h"] = [x.data_ptr() for x in hs]
-        srcs["out"] = [o.data_ptr() for o in outs]
+        if outs is not None:
+            srcs["out"] = [o.data_ptr() for o in outs]
+        if data is not None:
+            srcs["data"] = [x.data_ptr() for x in data]
+            srcs["inner"] = [inner.data_ptr() + 48 * i for i in range(ns)]
         srcs["n"] = lengths
         srcs["projections_start"] = self.projections_start_ind
         srcs["tdi_start"] = self.tdi_start_ind
@@ -333,7 +401,7 @@ class BatchedResponseTDI:
             else:
                 rc = lib.flr_batch_run(self._plan, src_p, ns, CHANNELS[self.tdi_chan], st)
         _lib.check(rc)
-        self._last_inputs = hs  # keep the inputs alive until the next call
+        self._last_inputs = (hs, data)  # keep the inputs alive until the next call
         return (outs, diags) if diagnostics else outs
 
     def _bucket(self, ns: int, waveforms: bool, diagnostics: bool) -> "BatchGraph":
