@@ -351,11 +351,11 @@ __device__ __forceinline__ DfWeights df_weights(df::f2 A, df::f2 e) {
 }
 
 __device__ __forceinline__ df::f2 df_tail_up(const DfWeights &w, df::f2 Ej, int j) {
-    return df::mul_raw(df::mul(w.c, Ej), df::rcp(df::add_big_float((float)j, w.e)));
+    return df::mul_raw(df::mul_raw(w.c, Ej), df::rcp(df::add_big_float((float)j, w.e)));
 }
 
 __device__ __forceinline__ df::f2 df_tail_dn(const DfWeights &w, df::f2 Ej, int j) {
-    return df::mul_raw(df::mul(w.c, Ej), df::rcp(df::add_big_float((float)j, w.ome)));
+    return df::mul_raw(df::mul_raw(w.c, Ej), df::rcp(df::add_big_float((float)j, w.ome)));
 }
 
 // Shared-memory df views of the staged input: value and first difference.
@@ -449,7 +449,7 @@ __device__ __forceinline__ df::f2 df_interp_real(const float2 *y, int d, df::f2 
     v = y[d];
     df::acc_fma(acc, df::mul_raw(w.A, w.e), {v.x, v.y});
     for (int j = 1; j < h; ++j) {
-        const df::f2 cE = df::mul(w.c, edf[j - 1]);
+        const df::f2 cE = df::mul_raw(w.c, edf[j - 1]);  // unnormalised: mul_raw accepts it
         float2 up = y[d + 1 + j], dn = y[d - j];
         df::acc_fma(acc, df::mul_raw(cE, df::rcp(df::add_big_float((float)j, w.e))),
                     {up.x, up.y});
@@ -517,7 +517,7 @@ __device__ __forceinline__ void df_interp_group(const float2 *y, const int off[3
     tap(df::mul_raw(w.A, w.ome), d + 1);
     tap(df::mul_raw(w.A, w.e), d);
     for (int j = 1; j < h; ++j) {
-        const df::f2 cE = df::mul(w.c, edf[j - 1]);
+        const df::f2 cE = df::mul_raw(w.c, edf[j - 1]);  // unnormalised: mul_raw accepts it
         tap(df::mul_raw(cE, df::rcp(df::add_big_float((float)j, w.e))), d + 1 + j);
         tap(df::mul_raw(cE, df::rcp(df::add_big_float((float)j, w.ome))), d - j);
     }
