@@ -233,6 +233,12 @@ typedef struct {
      * utils/utility.py:16-82, forms such products from the stored channels.) */
     const double *data;
     double *inner;
+    /* Optional output range (out_end <= out_begin = all of [tdi_start, n -
+     * tdi_start)): only the tiles overlapping [out_begin, out_end) are
+     * computed, with the same bits as a whole-source run (sample i is still at
+     * t0 + i / fs); the first and last tiles also write the zero edge zones.
+     * The taps may read h anywhere within the delays' reach of the range. */
+    long long out_begin, out_end;
 } flr_batch_source;
 
 typedef struct flr_batch_plan flr_batch_plan;

@@ -166,14 +166,15 @@ void make_groups(flr::FusedTdiSet &s) {
 // Staging layout: descriptors | tile prefix sums | waveform parameters |
 // chunk prefix sums, each part 256-byte aligned.
 struct StageLayout {
-    size_t tiles, gb, chunks, bytes;
+    size_t tiles, base, gb, chunks, bytes;
 };
 
 StageLayout stage_layout(int cap, bool waveforms) {
     auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
     StageLayout l;
     l.tiles = up(sizeof(flr::FusedSource) * (size_t)cap);
-    l.gb = up(l.tiles + sizeof(long) * ((size_t)cap + 1));
+    l.base = up(l.tiles + sizeof(long) * ((size_t)cap + 1));
+    l.gb = up(l.base + sizeof(long) * ((size_t)cap + 1));
     l.chunks = up(l.gb + (waveforms ? sizeof(flr::GbParams) * (size_t)cap : 0));
     l.bytes = l.chunks + (waveforms ? sizeof(long) * ((size_t)cap + 1) : 0);
     return l;
@@ -189,6 +190,7 @@ int fill_stage(const flr_batch_plan *plan, const flr_batch_source *sources, int 
     const int tile = plan->base.tile;
     flr::FusedSource *srcs = reinterpret_cast<flr::FusedSource *>(hs);
     long *tile_start = reinterpret_cast<long *>(hs + lay.tiles);
+    long *tile_base = reinterpret_cast<long *>(hs + lay.base);
     long *chunk_start = reinterpret_cast<long *>(hs + lay.chunks);
     long tiles = 0, chunks = 0;
     *diag = false;
@@ -230,11 +232,22 @@ int fill_stage(const flr_batch_plan *plan, const flr_batch_source *sources, int 
         d.d_tdi_out = s.d_tdi_out;
         d.data = s.data;
         d.inner = s.inner;
+        const long all_tiles = (long)((s.n - 2LL * s.tdi_start + tile - 1) / tile);
+        long first = 0, count = all_tiles;
+        if (s.out_end > s.out_begin) {
+            if (s.out_begin < s.tdi_start || s.out_end > s.n - s.tdi_start)
+                return fail(FLR_E_INVALID_ARGUMENT,
+                            "source " + std::to_string(i) +
+                                ": need tdi_start <= out_begin < out_end <= n - tdi_start");
+            first = (long)((s.out_begin - s.tdi_start) / tile);
+            count = (long)((s.out_end - s.tdi_start + tile - 1) / tile) - first;
+        }
+        tile_base[i] = tiles - first;
         *diag = *diag || s.y_out || s.d_rec_out || s.d_tdi_out;
         *inner = *inner || s.inner;
         std::memcpy(srcs + i, &d, sizeof(d));
         tile_start[i] = tiles;
-        tiles += (long)((s.n - 2LL * s.tdi_start + tile - 1) / tile);
+        tiles += count;
         if (gb) {
             chunk_start[i] = chunks;
             chunks += flr::gb_waveform_chunks((long)s.n);
@@ -252,6 +265,7 @@ int fill_stage(const flr_batch_plan *plan, const flr_batch_source *sources, int 
     }
     for (int i = num_sources; i <= cap; ++i) {
         tile_start[i] = tiles;
+        tile_base[i] = tiles;
         if (gb) chunk_start[i] = chunks;
     }
     return FLR_OK;
@@ -275,6 +289,7 @@ cudaError_t enqueue(const flr_batch_plan *plan, const unsigned char *h_stage,
     flr::FusedArgs a = plan->base;
     a.sources = d_src;
     a.tile_start = reinterpret_cast<const long *>(d_stage + lay.tiles);
+    a.tile_base = reinterpret_cast<const long *>(d_stage + lay.base);
     a.num_sources = cap;
     a.chan = chan;
     a.partial = partial;

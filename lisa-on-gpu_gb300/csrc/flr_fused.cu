@@ -577,7 +577,7 @@ __global__ void __launch_bounds__(kThreads, (kGrouped && !kDiag) ? 3 : 0)
             else
                 hi = mid - 1;
         }
-        const long tile_idx = wi - __ldg(a.tile_start + si);
+        const long tile_idx = wi - __ldg(a.tile_base + si);
         const FusedSource &src = a.sources[si];
         const long n = src.n;
         const int ps = src.ps, ts = src.ts;

@@ -87,6 +87,9 @@ struct FusedArgs {
     // with tile_start[s] <= w < tile_start[s + 1].  The total is read on the
     // device, so a captured launch can run batches of any lengths.
     const long *tile_start;
+    // tile_base[s] = tile_start[s] - (index of the first tile source s computes),
+    // so that work item w is tile w - tile_base[s] of its source
+    const long *tile_base;
     int num_sources;
     // per work item: the six partial inner products of its tile (inner-product
     // runs only; reduced per source by launch_inner_reduce)

@@ -74,7 +74,9 @@ class _Source(ctypes.Structure):
                 ("d_em_out", ctypes.c_void_p),
                 ("d_tdi_out", ctypes.c_void_p),
                 ("data", ctypes.c_void_p),
-                ("inner", ctypes.c_void_p)]
+                ("inner", ctypes.c_void_p),
+                ("out_begin", ctypes.c_longlong),
+                ("out_end", ctypes.c_longlong)]
 
 
 def _combinations(spec):
@@ -208,6 +210,16 @@ class BatchedResponseTDI:
         lib.flr_batch_plan_info(plan, info, 8)
         self.plan_info = dict(zip(("tile", "y_halo", "win_max", "y_max", "smem_bytes",
                                    "grid", "precision", "grouped"), list(info)))
+        self._ctor = dict(sampling_frequency=sampling_frequency, order=order, tdi=tdi,
+                          orbits=orbits, tdi_chan=tdi_chan, precision=precision,
+                          t_buffer=t_buffer, force_backend=self.device)
+        # input samples a tile's computation can read beyond its outputs: the
+        # link-stream halo plus the largest delay either way (light travel
+        # time and the spacecraft's distance from the Sun along k) and the taps
+        lmax = float(np.abs(np.asarray(orbits.pycppdetector_args[3], dtype=np.float64)).max())
+        self._reach = (self.plan_info["y_halo"]
+                       + int(np.ceil((lmax + max_sc * C_inv) * sampling_frequency))
+                       + (order + 1) // 2 + 16)
 
     def __del__(self):
         try:
@@ -220,7 +232,8 @@ class BatchedResponseTDI:
             pass
 
     def __call__(self, h: Sequence, lam, beta, t0=0.0, tdi_set=0, out: Optional[Sequence] = None,
-                 stream=None, diagnostics: bool = False, use_graph: bool = False):
+                 stream=None, diagnostics: bool = False, use_graph: bool = False,
+                 chunks: int = 1):
         """Evaluate the batch.
 
         Args:
@@ -236,6 +249,10 @@ class BatchedResponseTDI:
                 integer delays the kernel used (for the output samples).
             use_graph: run through the CUDA graph of this batch's size bucket
                 (captured on first use; see :meth:`graph`).
+            chunks: split each source's outputs into this many tile-aligned
+                launches alternating over two streams (and two plans), so that
+                one launch's last wave overlaps the next one's start; the same
+                bits as one launch.  For few, long sources.
         Returns:
             list of (3, n) tensors: rows X, Y, Z (or A, E, T / A, E and a
             zero third row); samples within t_buffer of either end are zero.
@@ -245,6 +262,11 @@ class BatchedResponseTDI:
         dev = self.device
         hs = [_as_device(x, dev, torch.complex128) for x in h]
         lengths = [len(x) for x in hs]
+        if chunks > 1 and not (diagnostics or use_graph):
+            outs = list(out) if out is not None else [
+                torch.empty((3, n), dtype=torch.float64, device=dev) for n in lengths]
+            self._pipeline(hs, None, outs, None, lam, beta, t0, tdi_set, chunks, stream)
+            return outs
         return self._run(hs, None, lengths, lam, beta, t0, tdi_set, out, stream, diagnostics,
                          self._bucket(len(hs), False, diagnostics) if use_graph else None)
 
@@ -323,6 +345,128 @@ class BatchedResponseTDI:
                   data=ds, inner=inner, write_out=False)
         return inner.view(ns, 2, 3), hs
 
+    def run_host(self, h: Sequence, lam, beta, t0=0.0, tdi_set=0, out: Optional[Sequence] = None,
+                 chunks: int = 4):
+        """Evaluate sources whose waveforms are in host memory, overlapping the
+        host-device copies with the computation.
+
+        Each source's output range is split into ``chunks`` tile-aligned
+        pieces.  A copy stream moves the input in pieces (each with the halo
+        its chunk's delays can reach), two compute streams with a plan each
+        run the chunks (a chunk's tail overlaps the next one's start) and a
+        second copy stream returns each chunk's channels as soon as it is
+        done.  Results are bit-identical to ``__call__`` on device copies of
+        the inputs (sample i is at t0 + i dt in every chunk).
+
+        Args:
+            h: host complex128 waveforms (pinned memory for asynchronous copies).
+            lam, beta, t0, tdi_set: as for __call__.
+            out: optional host (3, n) float64 tensors (pinned); allocated
+                pinned when omitted.
+        Returns:
+            the list of host output tensors; the current CUDA stream is made to
+            wait for them (synchronise it before reading them on the host).
+        """
+        ns = len(h)
+        lam = np.broadcast_to(np.asarray(lam, dtype=np.float64), (ns,))
+        beta = np.broadcast_to(np.asarray(beta, dtype=np.float64), (ns,))
+        t0 = np.broadcast_to(np.asarray(t0, dtype=np.float64), (ns,))
+        sets = np.broadcast_to(np.asarray(tdi_set, dtype=np.int64), (ns,))
+        hh = [torch.as_tensor(x) for x in h]
+        for i, x in enumerate(hh):
+            if x.device.type != "cpu" or x.dtype != torch.complex128 or x.ndim != 1 \
+                    or not x.is_contiguous():
+                raise ValueError(f"h[{i}] must be a contiguous 1-D complex128 host array")
+        outs = list(out) if out is not None else [
+            torch.empty((3, len(x)), dtype=torch.float64, pin_memory=True) for x in hh]
+        for i, (o, x) in enumerate(zip(outs, hh)):
+            if (tuple(o.shape) != (3, len(x)) or o.dtype != torch.float64
+                    or o.device.type != "cpu" or not o.is_contiguous()):
+                raise ValueError(f"out[{i}] must be a contiguous (3, {len(x)}) float64 host tensor")
+        self._pipeline(None, hh, None, outs, lam, beta, t0, sets, chunks, None)
+        return outs
+
+    def _pipeline(self, d_hs, host_hs, d_outs, host_outs, lam, beta, t0, tdi_set, chunks,
+                  stream):
+        """Chunked execution over two compute streams: each source's outputs in
+        `chunks` tile-aligned launches; with host inputs/outputs, a copy stream
+        brings each chunk's input (with the reach of its delays) and another
+        returns its channels.  The calling stream waits for the result."""
+        dev = self.device
+        host = host_hs is not None
+        ns = len(host_hs if host else d_hs)
+        lam = np.broadcast_to(np.asarray(lam, dtype=np.float64), (ns,))
+        beta = np.broadcast_to(np.asarray(beta, dtype=np.float64), (ns,))
+        t0 = np.broadcast_to(np.asarray(t0, dtype=np.float64), (ns,))
+        sets = np.broadcast_to(np.asarray(tdi_set, dtype=np.int64), (ns,))
+        plans = [self, self._twin()]
+        cur = stream if stream is not None else torch.cuda.current_stream(dev)
+        if not hasattr(self, "_side_streams"):
+            self._side_streams = [torch.cuda.Stream(device=dev) for _ in range(4)]
+        s_in, s_k0, s_k1, s_out = self._side_streams
+        s_comp = [s_k0, s_k1]
+        start = torch.cuda.Event()
+        start.record(cur)
+        for s_ in self._side_streams:
+            s_.wait_event(start)
+        tile, ts, reach = self.plan_info["tile"], self.tdi_start_ind, self._reach
+        k = 0
+        for i in range(ns):
+            if host:
+                n = len(host_hs[i])
+                d_h = torch.empty(n, dtype=torch.complex128, device=dev)
+                d_o = torch.empty((3, n), dtype=torch.float64, device=dev)
+                for s_ in self._side_streams:
+                    d_h.record_stream(s_)
+                    d_o.record_stream(s_)
+            else:
+                d_h, d_o = d_hs[i], d_outs[i]
+                n = len(d_h)
+                if (tuple(d_o.shape) != (3, n) or d_o.dtype != torch.float64 or not d_o.is_cuda
+                        or not d_o.is_contiguous()):
+                    raise ValueError(f"out[{i}] must be a contiguous (3, {n}) float64 CUDA tensor")
+            tiles = -(-(n - 2 * ts) // tile)
+            per = -(-tiles // max(1, min(int(chunks), tiles)))
+            ranges = [(ts + a * tile, min(ts + (a + per) * tile, n - ts))
+                      for a in range(0, tiles, per)]
+            done_in = 0
+            for c, (a, b) in enumerate(ranges):
+                last = c == len(ranges) - 1
+                comp = s_comp[k % 2]
+                if host:
+                    need = n if last else min(n, b + reach)
+                    ev_in = torch.cuda.Event()
+                    with torch.cuda.stream(s_in):
+                        if need > done_in:
+                            d_h[done_in:need].copy_(host_hs[i][done_in:need], non_blocking=True)
+                            done_in = need
+                        ev_in.record(s_in)
+                    comp.wait_event(ev_in)
+                plans[k % 2]._run([d_h], None, [n], lam[i:i + 1], beta[i:i + 1], t0[i:i + 1],
+                                  sets[i:i + 1], [d_o], comp, False, None, out_range=(a, b))
+                if host:
+                    ev_k = torch.cuda.Event()
+                    ev_k.record(comp)
+                    s_out.wait_event(ev_k)
+                    lo, hi = (0 if c == 0 else a), (n if last else b)
+                    with torch.cuda.stream(s_out):
+                        for r in range(3):
+                            host_outs[i][r, lo:hi].copy_(d_o[r, lo:hi], non_blocking=True)
+                k += 1
+        for s_ in (s_out,) if host else tuple(s_comp):
+            end = torch.cuda.Event()
+            end.record(s_)
+            cur.wait_event(end)
+
+    def _twin(self) -> "BatchedResponseTDI":
+        """A second plan with this one's configuration (own staging buffers),
+        for a second compute stream."""
+        if getattr(self, "_twin_plan", None) is None:
+            kw = dict(self._ctor)
+            kw["tile"] = self.plan_info["tile"]
+            self._twin_plan = BatchedResponseTDI(**kw)
+        return self._twin_plan
+
     def _check_data(self, data, lengths):
         ds = list(data)
         if len(ds) != len(lengths):
@@ -337,7 +481,7 @@ class BatchedResponseTDI:
 
     # -- internals ----------------------------------------------------------------
     def _run(self, hs, params, lengths, lam, beta, t0, tdi_set, out, stream, diagnostics, graph,
-             data=None, inner=None, write_out=True):
+             data=None, inner=None, write_out=True, out_range=None):
         ns = len(hs)
         dev = self.device
         lam = np.broadcast_to(np.asarray(lam, dtype=np.float64), (ns,))
@@ -361,6 +505,8 @@ class BatchedResponseTDI:
         srcs["h"] = [x.data_ptr() for x in hs]
         if outs is not None:
             srcs["out"] = [o.data_ptr() for o in outs]
+        if out_range is not None:
+            srcs["out_begin"], srcs["out_end"] = out_range
         if data is not None:
             srcs["data"] = [x.data_ptr() for x in data]
             srcs["inner"] = [inner.data_ptr() + 48 * i for i in range(ns)]
