@@ -152,13 +152,16 @@ class ResponseServer:
         num_streams: concurrent batches on the device.
         max_batch_samples / max_batch_sources: batch size limits.
         executor: override (tests); default drives the GPU.
+        keep_results: False drops each result once its request is done (only
+            the timings stay; ``result()`` then returns None): for load
+            tests whose clients do not read the channels.
     """
 
     def __init__(self, sampling_frequency, orbits=None, order=25,
                  tdi_sets=("1st generation", "2nd generation"), tdi_chan="XYZ",
                  precision="mixed", t_buffer=10000.0, memory_budget=160e9, num_streams=2,
                  max_batch_samples=2**26, max_batch_sources=512, force_backend=None,
-                 executor=None):
+                 executor=None, keep_results=True):
         self.tdi_start_ind = int(t_buffer * sampling_frequency)
         self.budget = int(memory_budget)
         self.max_batch_samples = int(max_batch_samples)
@@ -173,6 +176,7 @@ class ResponseServer:
                 orbits if orbits is not None else EqualArmlengthOrbits), order, tdi_sets,
                 tdi_chan, precision, t_buffer, num_streams, device)
         self.executor = executor
+        self.keep_results = bool(keep_results)
         self._inbox: "queue.SimpleQueue[Request]" = queue.SimpleQueue()
         self._wake = threading.Event()
         self._stop = False
@@ -231,7 +235,7 @@ class ResponseServer:
                     outs = self.executor.results(handle)
                     done = time.perf_counter()
                     for r, o in zip(batch, outs):
-                        r.result_value = o
+                        r.result_value = o if self.keep_results else None
                         r.t_done = done
                         self.used -= r.footprint
                         self.completed.append(r)
