@@ -275,6 +275,78 @@ __device__ __forceinline__ EmitterSide emitter_mixed(const OrbitTables &o, doubl
     return e;
 }
 
+// The exact flavour's link geometry split into its receiver side (shared by
+// the two links a spacecraft receives) and its emitter side: the operations
+// of link_geometry() in the same order, so the same bits.
+struct ReceiverF64 {
+    int d_rec;
+    double e_rec;
+    double x_rec[3];
+};
+
+__device__ __forceinline__ ReceiverF64 receiver_f64(const OrbitTables &o, int sc, double t,
+                                                    double t_first, double fs,
+                                                    const double k[3]) {
+    ReceiverF64 r;
+    position(o, t, sc, r.x_rec);
+    const double kx_rec = dot3(k, r.x_rec);
+    const double delay_rec = t - kx_rec * kCInv;
+    split_delay(delay_rec, t_first, fs, r.d_rec, r.e_rec);
+    return r;
+}
+
+struct EmitterF64 {
+    int d_em;
+    double e_em;
+    double xi_p, xi_c, k_dot_n;
+};
+
+__device__ __forceinline__ EmitterF64 emitter_f64(const OrbitTables &o, int slot, double t,
+                                                  const double x_rec[3], double t_first,
+                                                  double fs, const double k[3],
+                                                  const double u[3], const double v[3]) {
+    EmitterF64 e;
+    const double L = light_travel_time(o, t, slot);
+    const double t_em = t - L;
+    double x_em[3], n[3];
+    position(o, t_em, o.sc_e[slot], x_em);
+    double norm = 0.0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        n[c] = x_rec[c] - x_em[c];
+        norm += n[c] * n[c];
+    }
+    norm = sqrt(norm);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) n[c] = n[c] / norm;
+    const double un = dot3(u, n), vn = dot3(v, n);
+    e.xi_p = 0.5 * ((un * un) - (vn * vn));
+    e.xi_c = un * vn;
+    e.k_dot_n = dot3(k, n);
+    const double kx_em = dot3(k, x_em);
+    const double delay_em = t_em - kx_em * kCInv;
+    split_delay(delay_em, t_first, fs, e.d_em, e.e_em);
+    return e;
+}
+
+// Exact complex interpolation at (d, eps) from the staged raw window when its
+// taps lie in it, else from global memory (the same values); false when the
+// taps leave the input.
+__device__ __forceinline__ bool c128_any(const double2 *hraw, long wlo, int W, const double2 *hg,
+                                         long n, int d, double eps, double A,
+                                         const LagrangeTables &lt, double &hp, double &hc) {
+    const long lo = (long)d - (lt.h - 1), hi = (long)d + lt.h;
+    if (lo >= wlo && hi < wlo + W) {
+        lagrange_c128(SharedC128{hraw}, (int)(d - wlo), eps, A, lt, hp, hc);
+        return true;
+    }
+    if (lo >= 0 && hi < n) {
+        lagrange_c128(GlobalC128{hg}, d, eps, A, lt, hp, hc);
+        return true;
+    }
+    return false;
+}
+
 // 1/sqrt(x) in df: hardware approximation and one Newton step,
 // r = r0 + r0 (1 - x r0^2) / 2; relative error ~1e-14.
 __device__ __forceinline__ df::f2 df_rsqrt(df::f2 x) {
@@ -824,6 +896,54 @@ __global__ void __launch_bounds__(kThreads, (kGrouped && !kDiag) ? 3 : 0)
                     y32[slot * a.y_max + jj] = make_float2(yv.hi, yv.lo);
                     if (kDiag && own && src.y_out)
                         src.y_out[(long)slot * n + j] = df::to_double(yv) / scale;
+                }
+            }
+        } else if (!kMixed && a.rx_shared) {
+            // exact flavour: one (receiver, sample) item, the receiver side
+            // shared by its two links
+            for (int it = tid; it < 3 * Y; it += kThreads) {
+                const int r = it / Y;
+                const int jj = it - r * Y;
+                const long j = ya + jj;
+                if (j < yfirst || j >= ylast) {  // the reference's y_gw is zero there
+                    y64[a.rx_slot[r][0] * a.y_max + jj] = 0.0;
+                    y64[a.rx_slot[r][1] * a.y_max + jj] = 0.0;
+                    continue;
+                }
+                const double t = t0 + (double)j * a.dt;
+                const bool own = (j >= o0 && j < o1);
+                const ReceiverF64 rs = receiver_f64(a.orb, a.rx_sc[r], t, t0, a.fs, k);
+                double A_r, hp_r = 0.0, hc_r = 0.0;
+                const bool okA_r = prefactor(a.lt, rs.e_rec, A_r);
+                const bool okT_r = okA_r && c128_any(hraw, wlo, W, src.h, n, rs.d_rec, rs.e_rec,
+                                                     A_r, a.lt, hp_r, hc_r);
+                for (int q = 0; q < 2; ++q) {
+                    const int slot = a.rx_slot[r][q];
+                    const EmitterF64 es = emitter_f64(a.orb, slot, t, rs.x_rec, t0, a.fs, k, u, v);
+                    if (kDiag && own && src.d_rec_out) {
+                        src.d_rec_out[(long)slot * n + j] = rs.d_rec;
+                        src.d_em_out[(long)slot * n + j] = es.d_em;
+                    }
+                    double A_e, out;
+                    const bool okA_e = prefactor(a.lt, es.e_em, A_e);
+                    if (!(okA_r && okA_e)) {
+                        raise_status(a.orb.status, kStatusAIndex);
+                        out = qnan();
+                    } else {
+                        double hp_e, hc_e;
+                        const bool okT_e = c128_any(hraw, wlo, W, src.h, n, es.d_em, es.e_em,
+                                                    A_e, a.lt, hp_e, hc_e);
+                        if (okT_r && okT_e) {
+                            double pre = 1. / (1. - es.k_dot_n);
+                            double big = (hp_e - hp_r) * es.xi_p + (hc_e - hc_r) * es.xi_c;
+                            out = pre * big;
+                        } else {
+                            raise_status(a.orb.status, kStatusTap);
+                            out = qnan();
+                        }
+                    }
+                    y64[slot * a.y_max + jj] = out;
+                    if (kDiag && own && src.y_out) src.y_out[(long)slot * n + j] = out;
                 }
             }
         } else
