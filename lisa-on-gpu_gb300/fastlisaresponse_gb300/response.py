@@ -472,12 +472,21 @@ class ResponseWrapper:
     t_buffer=10000.0, flip_hx=False, remove_sky_coords=False,
     is_ecliptic_latitude=True, force_backend=None, remove_garbage=True,
     n_overide=None, orbits=EqualArmlengthOrbits, **kwargs for pyResponseTDI.
+
+    One addition, off by default: ``precision="fp64"`` or ``"mixed"`` computes
+    the channels with the fused kernel (:class:`BatchedResponseTDI`; one
+    launch, the link streams never stored) instead of get_projections +
+    get_tdi_delays: "fp64" gives the same bits, "mixed" the bit-exact integer
+    delays and the channels within 1e-6 relative L2 at ~16x the speed.
+    ``chunks`` splits that launch (long observations; see
+    BatchedResponseTDI.__call__).
     """
 
     def __init__(self, waveform_gen, Tobs, dt, index_lambda, index_beta, t0=0.0,
                  t_buffer=10000.0, flip_hx=False, remove_sky_coords=False,
                  is_ecliptic_latitude=True, force_backend=None, remove_garbage=True,
-                 n_overide=None, orbits: Optional[Orbits] = EqualArmlengthOrbits, **kwargs):
+                 n_overide=None, orbits: Optional[Orbits] = EqualArmlengthOrbits,
+                 precision: Optional[str] = None, chunks: int = 1, **kwargs):
         self.waveform_gen = waveform_gen
         self.index_lambda = index_lambda
         self.index_beta = index_beta
@@ -504,6 +513,18 @@ class ResponseWrapper:
         self.response_model = pyResponseTDI(self.sampling_frequency, self.n, orbits=orbits,
                                             force_backend=force_backend, **kwargs)
         self.Tobs = (self.n * self.response_model.dt) / YRSID_SI
+        self.precision = precision
+        self.chunks = int(chunks)
+        self._fused = None
+        if precision is not None:
+            from .batch import BatchedResponseTDI
+
+            self._fused = BatchedResponseTDI(
+                self.sampling_frequency, order=kwargs.get("order", 25),
+                tdi=kwargs.get("tdi", "1st generation"), orbits=orbits,
+                tdi_chan=kwargs.get("tdi_chan", "XYZ"), precision=precision,
+                t_buffer=t_buffer, force_backend=self.response_model.device)
+            self._nchan = 2 if kwargs.get("tdi_chan", "XYZ") == "AE" else 3
 
     @property
     def xp(self):
@@ -531,10 +552,14 @@ class ResponseWrapper:
         h = self.waveform_gen(*args, **kwargs)
         if self.flip_hx:
             h = h.real - 1j * h.imag if not isinstance(h, torch.Tensor) else h.conj().resolve_conj()
-        self.response_model.get_projections(h, lam, beta, t0=self.t0, t_buffer=self.t_buffer)
-        tdi_out = self.response_model.get_tdi_delays()
-        out = list(tdi_out)
-        ts = self.response_model.tdi_start_ind
+        if self._fused is not None:
+            chans = self._fused([h], lam, beta, t0=self.t0, chunks=self.chunks)[0]
+            out = [chans[c] for c in range(self._nchan)]
+        else:
+            self.response_model.get_projections(h, lam, beta, t0=self.t0,
+                                                t_buffer=self.t_buffer)
+            out = list(self.response_model.get_tdi_delays())
+        ts = (self._fused or self.response_model).tdi_start_ind
         if self.remove_garbage is True:
             for i in range(len(out)):
                 out[i] = out[i][ts:-ts]
