@@ -445,6 +445,7 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
     const int spread = (int)std::ceil(2.0 * lmax * sampling_frequency) + 2;
     p->base.tile = tile;
     p->base.y_halo = y_halo;
+    p->base.y_halo_hi = std::min(y_halo, h + 3);
     p->base.y_max = tile + 2 * y_halo;
     p->base.win_max = tile + 2 * y_halo + 2 * h + spread + 2 * 4 + 16;
     p->smem = flr::fused_smem_bytes(p->mixed, p->base.win_max, p->base.y_max);

@@ -688,7 +688,7 @@ __global__ void __launch_bounds__(kThreads, (kGrouped && !kDiag) ? 3 : 0)
                     for (long i = n - ts + tid; i < n; i += kThreads) src.out[c * n + i] = 0.0;
         }
         const long ya = max(o0 - a.y_halo, 0L);
-        const long yb = min(o1 + a.y_halo, n);
+        const long yb = min(o1 + a.y_halo_hi, n);
         const long yfirst = max(ya, (long)ps), ylast = min(yb, n - ps);  // y computed here
         const int Y = (int)(yb - ya);
 

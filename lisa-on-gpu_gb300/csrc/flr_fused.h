@@ -98,7 +98,9 @@ struct FusedArgs {
     int num_sets;
     const float4 *a_tab;       // per A-table knot: (A hi, A lo, dA hi, dA lo), dA = A[k+1]-A[k]
     int tile;                  // output samples per work item
-    int y_halo;                // link-stream samples computed on each side of a tile
+    int y_halo;                // link-stream samples computed before a tile
+    int y_halo_hi;             // and after it: TDI delays only look back, so the taps
+                               // of a tile's last sample reach h samples past it
     int win_max;               // capacity of the staged input window [samples]
     int y_max;                 // capacity of one staged link row [samples]
     double fs;                 // sampling frequency
