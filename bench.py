@@ -77,6 +77,7 @@ DEFAULT_WORKLOAD = "1yr_dt5_gen2"
 CPU_SLICE = 2**16  # samples per source in the CPU measurements
 HEADLINE_CHUNKS = 8  # launches per headline step (two streams: last waves overlap)
 E2E_CHUNKS = 8       # pieces of the end-to-end step's source (copy/compute overlap)
+SERVE_BATCH_SAMPLES = 2**23  # samples per serving batch at most (the server's default)
 
 
 # ----------------------------------------------------------------------------- setup
@@ -555,7 +556,8 @@ def run_serving_section(args, device):
 
     def run(rate):
         with flr.ResponseServer(1 / dt, orbits=orb, num_streams=2, force_backend=device,
-                                keep_results=False) as srv:
+                                keep_results=False,
+                                max_batch_samples=SERVE_BATCH_SAMPLES) as srv:
             srv.submit(params[0], int(lengths[0]), int(sets[0])).result(timeout=60)  # warm-up
             srv.completed.clear()
             arrivals = (np.cumsum(rng.exponential(1.0 / rate, count)) if rate
