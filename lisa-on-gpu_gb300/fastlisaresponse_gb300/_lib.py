@@ -90,5 +90,34 @@ def check(rc: int) -> None:
     raise FLRError(msg)
 
 
+class nvtx_range:
+    """NVTX range around a library call (visible in Nsight Systems); a no-op
+    where NVTX is unavailable."""
+
+    def __init__(self, name: str):
+        self.name = name
+        self.pushed = False
+
+    def __enter__(self):
+        try:
+            import torch
+
+            torch.cuda.nvtx.range_push(self.name)
+            self.pushed = True
+        except Exception:
+            self.pushed = False
+        return self
+
+    def __exit__(self, *exc):
+        if self.pushed:
+            try:
+                import torch
+
+                torch.cuda.nvtx.range_pop()
+            except Exception:
+                pass
+        return False
+
+
 def describe_status(bits: int) -> str:
     return ", ".join(text for bit, text in STATUS_BITS.items() if bits & bit) or "ok"

@@ -539,7 +539,7 @@ class BatchedResponseTDI:
         src_p = srcs.ctypes.data_as(ctypes.POINTER(_Source))
         gb_p = gbs.ctypes.data_as(ctypes.POINTER(_GbParams)) if gbs is not None else None
         st = ctypes.c_void_p(stream.cuda_stream)
-        with torch.cuda.device(dev):
+        with torch.cuda.device(dev), _lib.nvtx_range(f"flr.batch[{ns}]"):
             if graph is not None:
                 rc = lib.flr_batch_graph_launch(graph._graph, src_p, gb_p, ns, st)
             elif gbs is not None:

@@ -31,6 +31,7 @@ try:
 except ImportError:  # pragma: no cover
     torch = None
 
+from . import _lib
 from .binding import LISAResponseWrap, OrbitsWrap
 from .orbits import EqualArmlengthOrbits, Orbits
 from .utils import AET
@@ -400,7 +401,7 @@ class pyResponseTDI:
             raise ValueError(f"input_in has {len(input_in)} samples, fewer than num_pts="
                              f"{self.num_pts}")
         y_gw = torch.zeros((self.nlinks * self.num_pts,), dtype=torch.float64, device=dev)
-        with torch.cuda.device(dev):
+        with torch.cuda.device(dev), _lib.nvtx_range("flr.get_response"):
             self.response_gen(y_gw, t_data, k_in, u_in, v_in, self.dt, len(input_in), input_in,
                               len(input_in), self.order, self.sampling_frequency,
                               self.buffer_integer, self.A_in, self.deps, len(self.A_in),
@@ -441,7 +442,7 @@ class pyResponseTDI:
                              "determine projections.")
         self.delayed_links_flat = self.delayed_links_flat.flatten()
         t_data = t0 + torch.arange(self.y_gw_length, dtype=torch.float64, device=dev) * self.dt
-        with torch.cuda.device(dev):
+        with torch.cuda.device(dev), _lib.nvtx_range("flr.get_tdi_delays"):
             self.tdi_gen(self.delayed_links_flat, self.y_gw_flat, self.y_gw_length, self.num_pts,
                          t_data, self.unit_starts, self.unit_lengths, self.tdi_base_links,
                          self.tdi_link_combinations, self.tdi_signs, self.channels,
