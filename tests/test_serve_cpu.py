@@ -120,3 +120,15 @@ def test_invalid_requests_are_rejected():
             srv.submit(_params(0), 1500)
     finally:
         srv.close()
+
+
+def test_dropped_results_keep_timings():
+    """keep_results=False (load tests): results are released as requests
+    complete, the timings and stats stay."""
+    ex = FakeExecutor()
+    with ResponseServer(0.1, executor=ex, memory_budget=1e12, keep_results=False) as srv:
+        reqs = [srv.submit(_params(i), 3000 + i) for i in range(12)]
+        for r in reqs:
+            assert r.result(timeout=10) is None
+    assert all(r.done() and r.latency >= 0 for r in reqs)
+    assert srv.stats()["requests"] == 12
