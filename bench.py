@@ -74,7 +74,7 @@ WORKLOADS = {
         dt=10.0, n=2**18, orbits="equal", tdi="1st generation", order=25),
 }
 DEFAULT_WORKLOAD = "1yr_dt5_gen2"
-CPU_SLICE = 2**16  # samples per source in the CPU measurements
+CPU_SLICE = 2**20  # samples per source in the CPU measurements (~3 s per pass on one core)
 HEADLINE_CHUNKS = 8  # launches per headline step (two streams: last waves overlap)
 E2E_CHUNKS = 8       # pieces of the end-to-end step's source (copy/compute overlap)
 SERVE_BATCH_SAMPLES = 2**23  # samples per serving batch at most (the server's default)
