@@ -97,6 +97,17 @@ __device__ __forceinline__ f2 rcp(f2 b) {
     return {r0, r0 * t};
 }
 
+// a / b for b in [1, 64): q0 = a.hi / b.hi from the hardware reciprocal,
+// corrected once by the df residual, q = q0 + r0 (a - q0 b); relative error
+// about 1e-13.  Not normalised.
+__device__ __forceinline__ f2 div_raw(f2 a, f2 b) {
+    const float r0 = rcp_approx(b.hi);
+    const float q0 = a.hi * r0;
+    float res = __fmaf_rn(-q0, b.hi, a.hi);
+    res = __fmaf_rn(-q0, b.lo, res);
+    res = res + a.lo;
+    return {q0, r0 * res};
+}
 // Dot2 accumulator (Ogita-Rump-Oishi): sum of df products.
 struct Acc {
     float s;    // running FP32 sum of the high parts

@@ -423,11 +423,11 @@ __device__ __forceinline__ DfWeights df_weights(df::f2 A, df::f2 e) {
 }
 
 __device__ __forceinline__ df::f2 df_tail_up(const DfWeights &w, df::f2 Ej, int j) {
-    return df::mul_raw(df::mul_raw(w.c, Ej), df::rcp(df::add_big_float((float)j, w.e)));
+    return df::div_raw(df::mul_raw(w.c, Ej), df::add_big_float((float)j, w.e));
 }
 
 __device__ __forceinline__ df::f2 df_tail_dn(const DfWeights &w, df::f2 Ej, int j) {
-    return df::mul_raw(df::mul_raw(w.c, Ej), df::rcp(df::add_big_float((float)j, w.ome)));
+    return df::div_raw(df::mul_raw(w.c, Ej), df::add_big_float((float)j, w.ome));
 }
 
 // Shared-memory df views of the staged input: value and first difference.
@@ -510,24 +510,27 @@ __device__ __forceinline__ bool df_interp_c128_any(const float4 *hdf, const floa
 }
 
 // Real interpolation around sample d of a staged df link row, compensated dot
-// product (Dot2).
+// products (Dot2).  The common factor c = A eps (1 - eps) of the outer taps
+// is applied once to their sum, sum_j E_j (y_up/(j + eps) + y_dn/(j + 1 - eps)),
+// whose terms are df quotients: per tap one division instead of a reciprocal
+// and two products.
 __device__ __forceinline__ df::f2 df_interp_real(const float2 *y, int d, df::f2 A, df::f2 eps,
                                                  const df::f2 *edf, int h) {
     const DfWeights w = df_weights(A, eps);
-    df::Acc acc;
+    df::Acc acc, tail;
     df::acc_init(acc);
+    df::acc_init(tail);
     float2 v = y[d + 1];
     df::acc_fma(acc, df::mul_raw(w.A, w.ome), {v.x, v.y});
     v = y[d];
     df::acc_fma(acc, df::mul_raw(w.A, w.e), {v.x, v.y});
     for (int j = 1; j < h; ++j) {
-        const df::f2 cE = df::mul_raw(w.c, edf[j - 1]);  // unnormalised: mul_raw accepts it
+        const df::f2 Ej = edf[j - 1];
         float2 up = y[d + 1 + j], dn = y[d - j];
-        df::acc_fma(acc, df::mul_raw(cE, df::rcp(df::add_big_float((float)j, w.e))),
-                    {up.x, up.y});
-        df::acc_fma(acc, df::mul_raw(cE, df::rcp(df::add_big_float((float)j, w.ome))),
-                    {dn.x, dn.y});
+        df::acc_fma(tail, df::div_raw(Ej, df::add_big_float((float)j, w.e)), {up.x, up.y});
+        df::acc_fma(tail, df::div_raw(Ej, df::add_big_float((float)j, w.ome)), {dn.x, dn.y});
     }
+    df::acc_add(acc, df::mul(w.c, df::acc_value(tail)));
     return df::acc_value(acc);
 }
 
@@ -590,8 +593,8 @@ __device__ __forceinline__ void df_interp_group(const float2 *y, const int off[3
     tap(df::mul_raw(w.A, w.e), d);
     for (int j = 1; j < h; ++j) {
         const df::f2 cE = df::mul_raw(w.c, edf[j - 1]);  // unnormalised: mul_raw accepts it
-        tap(df::mul_raw(cE, df::rcp(df::add_big_float((float)j, w.e))), d + 1 + j);
-        tap(df::mul_raw(cE, df::rcp(df::add_big_float((float)j, w.ome))), d - j);
+        tap(df::div_raw(cE, df::add_big_float((float)j, w.e)), d + 1 + j);
+        tap(df::div_raw(cE, df::add_big_float((float)j, w.ome)), d - j);
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
