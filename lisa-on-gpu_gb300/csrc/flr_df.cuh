@@ -58,12 +58,23 @@ __device__ __forceinline__ f2 add(f2 a, f2 b) {
     return fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
 }
 
+// a + b without the final renormalisation: for operands that cannot cancel
+// (|lo| of the result stays within a few ulp of hi).
+__device__ __forceinline__ f2 add_raw(f2 a, f2 b) {
+    f2 s = two_sum(a.hi, b.hi);
+    return {s.hi, s.lo + (a.lo + b.lo)};
+}
 // a - b, result normalised.
 __device__ __forceinline__ f2 sub(f2 a, f2 b) {
     f2 s = two_sum(a.hi, -b.hi);
     return fast_two_sum(s.hi, s.lo + (a.lo - b.lo));
 }
 
+// 1 - a for 0 <= a.hi <= 1 (FastTwoSum applies); not normalised.
+__device__ __forceinline__ f2 one_minus(f2 a) {
+    f2 s = fast_two_sum(1.0f, -a.hi);
+    return {s.hi, s.lo - a.lo};
+}
 // a * b with the lo*lo term dropped (relative error ~2^-46); not normalised
 // (|lo| is a few ulp of hi at most), which the consumers below accept.
 __device__ __forceinline__ f2 mul_raw(f2 a, f2 b) {

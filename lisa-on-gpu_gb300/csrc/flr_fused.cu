@@ -401,7 +401,8 @@ __device__ __forceinline__ df::f2 prefactor_df(const float4 *tab, int num_A, df:
     ind = min(max(ind, 0), num_A - 2);
     const df::f2 frac = df::fast_two_sum(q.hi - (float)ind, q.lo);
     const float4 t = __ldg(tab + ind);
-    return df::add({t.x, t.y}, df::mul_raw(frac, {t.z, t.w}));
+    // A >= 1 and the segment's change is ~1e-3 of it: no cancellation
+    return df::add_raw({t.x, t.y}, df::mul_raw(frac, {t.z, t.w}));
 }
 
 // --------------------------------------------- double-float interpolation ----
@@ -417,7 +418,7 @@ __device__ __forceinline__ DfWeights df_weights(df::f2 A, df::f2 e) {
     DfWeights w;
     w.A = A;
     w.e = e;
-    w.ome = df::sub({1.0f, 0.0f}, e);
+    w.ome = df::one_minus(e);
     w.c = df::mul(df::mul(A, e), w.ome);
     return w;
 }
@@ -432,15 +433,17 @@ __device__ __forceinline__ df::f2 df_tail_dn(const DfWeights &w, df::f2 Ej, int 
 
 // Shared-memory df views of the staged input: value and first difference.
 struct DfShared {
-    const float4 *x;   // (re_hi, re_lo, im_hi, im_lo)
-    const float4 *dx;  // x[k+1] - x[k]
-    __device__ __forceinline__ float4 val(long k) const { return x[k]; }
-    __device__ __forceinline__ float4 diff(long k) const { return dx[k]; }
+    using index_t = int;  // window offsets: 32-bit shared-memory addressing
+    const float4 *x;      // (re_hi, re_lo, im_hi, im_lo)
+    const float4 *dx;     // x[k+1] - x[k]
+    __device__ __forceinline__ float4 val(int k) const { return x[k]; }
+    __device__ __forceinline__ float4 diff(int k) const { return dx[k]; }
 };
 
 // The same views computed on the fly from global memory (used when a tap
 // window falls outside the staged window).
 struct DfGlobal {
+    using index_t = long;
     const double2 *h;
     double scale;
     __device__ __forceinline__ float4 val(long k) const {
@@ -457,7 +460,8 @@ struct DfGlobal {
 
 // Complex interpolation around sample d of the source, by summation by parts.
 template <class Src>
-__device__ __forceinline__ void df_interp_c128_sbp(const Src &src, long d, df::f2 A, df::f2 eps,
+__device__ __forceinline__ void df_interp_c128_sbp(const Src &src, typename Src::index_t d,
+                                                   df::f2 A, df::f2 eps,
                                                    const df::f2 *edf, int h, df::f2 &re,
                                                    df::f2 &im) {
     const DfWeights w = df_weights(A, eps);
@@ -465,7 +469,8 @@ __device__ __forceinline__ void df_interp_c128_sbp(const Src &src, long d, df::f
     df::Acc sre, sim;
     df::acc_init(sre);
     df::acc_init(sim);
-    auto step = [&](df::f2 W, long k) {
+    using index_t = typename Src::index_t;
+    auto step = [&](df::f2 W, index_t k) {
         P = df::add(P, W);
         float4 dx = src.diff(k);
         df::acc_fma(sre, P, {dx.x, dx.y});
@@ -474,7 +479,7 @@ __device__ __forceinline__ void df_interp_c128_sbp(const Src &src, long d, df::f
     for (int j = h - 1; j >= 1; --j) step(df_tail_dn(w, edf[j - 1], j), d - j);
     step(df::mul_raw(w.A, w.e), d);
     df::f2 W_last;
-    long last;
+    index_t last;
     if (h == 1) {
         W_last = df::mul_raw(w.A, w.ome);
         last = d + 1;
@@ -499,7 +504,7 @@ __device__ __forceinline__ bool df_interp_c128_any(const float4 *hdf, const floa
                                                    int h, df::f2 &re, df::f2 &im) {
     const long lo = (long)d - (h - 1), hi = (long)d + h;
     if (lo >= wlo && hi + 1 < wlo + W) {
-        df_interp_c128_sbp(DfShared{hdf, dh}, d - wlo, A, eps, edf, h, re, im);
+        df_interp_c128_sbp(DfShared{hdf, dh}, (int)(d - wlo), A, eps, edf, h, re, im);
         return true;
     }
     if (lo >= 0 && hi + 1 < n) {
@@ -977,8 +982,8 @@ __global__ void __launch_bounds__(kThreads, (kGrouped && !kDiag) ? 3 : 0)
                 df::f2 re_r, im_r, re_e, im_e;
                 if (lo >= wlo && hi + 1 < wlo + W) {
                     const DfShared s{hdf, dh};
-                    df_interp_c128_sbp(s, g.d_rec - wlo, A_r, e_r, edf, h, re_r, im_r);
-                    df_interp_c128_sbp(s, g.d_em - wlo, A_e, e_e, edf, h, re_e, im_e);
+                    df_interp_c128_sbp(s, (int)(g.d_rec - wlo), A_r, e_r, edf, h, re_r, im_r);
+                    df_interp_c128_sbp(s, (int)(g.d_em - wlo), A_e, e_e, edf, h, re_e, im_e);
                 } else if (lo >= 0 && hi + 1 < n) {
                     const DfGlobal s{src.h, scale};
                     df_interp_c128_sbp(s, g.d_rec, A_r, e_r, edf, h, re_r, im_r);
