@@ -252,11 +252,13 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
                           const flr_tdi_units *sets, int num_sets, int precision, int tile,
                           flr_batch_plan **out);
 int flr_batch_plan_destroy(flr_batch_plan *plan);
-/* info[0..7] = tile, y halo, input window capacity, link row capacity, shared
- * memory bytes per block, persistent grid size, precision, and 1 when the
- * mixed kernel evaluates the TDI units in equal-delay groups (equal-arm
- * orbits: units with delay lists of equal length share one interpolation of
- * their combined link rows). */
+/* info[0..8] = tile, y halo, input window capacity, link row capacity, shared
+ * memory bytes per block, persistent grid size, precision, 1 when the mixed
+ * kernel evaluates the TDI units in equal-delay groups (equal-arm orbits:
+ * units with delay lists of equal length share one interpolation of their
+ * combined link rows), and the first outer tap j of the TDI interpolations
+ * that the mixed kernel evaluates in FP32 (its weights are small enough; the
+ * half-width h when none). */
 int flr_batch_plan_info(const flr_batch_plan *plan, int *info, int n_info);
 
 /* Evaluate `num_sources` sources (host array of descriptors) on `stream`. */

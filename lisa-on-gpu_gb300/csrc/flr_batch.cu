@@ -461,6 +461,14 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
         release(p);
         return cuda_fail(err, "reading the A table");
     }
+    std::vector<double> e_host(std::max(h - 1, 1), 0.0);
+    if (h > 1) {
+        err = cudaMemcpy(e_host.data(), E_in, sizeof(double) * (h - 1), cudaMemcpyDefault);
+        if (err != cudaSuccess) {
+            release(p);
+            return cuda_fail(err, "reading the E table");
+        }
+    }
     std::vector<float4> a_tab(num_A);
     for (int i = 0; i < num_A; ++i) {
         const double a = a_host[i];
@@ -517,6 +525,24 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
     b.lt.deps = deps;
     b.lt.num_A = num_A;
     b.lt.h = h;
+    // Outer TDI taps in FP32 (mixed flavour): with c = A eps (1 - eps) <= max A / 4
+    // and both denominators j + eps, j + 1 - eps >= j, the taps j >= h_df weigh
+    // at most 2 sum_j c_max |E_j| / j <= 5e-6 of the link values together, so
+    // their FP32 evaluation (relative error ~2e-7) adds at most ~1e-12 of max|y|
+    // to a unit's interpolation, against ~1e-14 from the double-float taps and
+    // an error budget of ~1e-11 (1e-6 relative on a 2nd-generation channel at
+    // 1e-4 Hz, 3e-4 of the link amplitude).  Order 25: taps 10..12; order 45:
+    // 14..22.
+    b.h_df = h;
+    if (p->mixed) {
+        double a_max = 0.0, outer = 0.0;
+        for (int i = 0; i < num_A; ++i) a_max = std::max(a_max, std::fabs(a_host[i]));
+        for (int j = h - 1; j >= 1; --j) {
+            outer += 2.0 * 0.25 * a_max * std::fabs(e_host[j - 1]) / j;
+            if (outer > 5e-6) break;
+            b.h_df = j;
+        }
+    }
     b.sets = reinterpret_cast<const flr::FusedTdiSet *>(static_cast<char *>(p->d_tables) +
                                                        set_off);
     b.num_sets = num_sets;
@@ -561,7 +587,7 @@ int flr_batch_plan_info(const flr_batch_plan *plan, int *info, int n_info) {
     const int vals[] = {plan->base.tile, plan->base.y_halo, plan->base.win_max,
                         plan->base.y_max, (int)plan->smem, plan->grid_max,
                         plan->mixed ? FLR_PRECISION_MIXED : FLR_PRECISION_FP64,
-                        plan->grouped ? 1 : 0};
+                        plan->grouped ? 1 : 0, plan->base.h_df};
     for (int i = 0; i < n_info && i < (int)(sizeof(vals) / sizeof(int)); ++i) info[i] = vals[i];
     return FLR_OK;
 }

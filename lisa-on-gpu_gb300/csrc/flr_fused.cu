@@ -520,7 +520,7 @@ __device__ __forceinline__ bool df_interp_c128_any(const float4 *hdf, const floa
 // whose terms are df quotients: per tap one division instead of a reciprocal
 // and two products.
 __device__ __forceinline__ df::f2 df_interp_real(const float2 *y, int d, df::f2 A, df::f2 eps,
-                                                 const df::f2 *edf, int h) {
+                                                 const df::f2 *edf, int h, int h_df) {
     const DfWeights w = df_weights(A, eps);
     df::Acc acc, tail;
     df::acc_init(acc);
@@ -529,12 +529,21 @@ __device__ __forceinline__ df::f2 df_interp_real(const float2 *y, int d, df::f2 
     df::acc_fma(acc, df::mul_raw(w.A, w.ome), {v.x, v.y});
     v = y[d];
     df::acc_fma(acc, df::mul_raw(w.A, w.e), {v.x, v.y});
-    for (int j = 1; j < h; ++j) {
+    for (int j = 1; j < h_df; ++j) {
         const df::f2 Ej = edf[j - 1];
         float2 up = y[d + 1 + j], dn = y[d - j];
         df::acc_fma(tail, df::div_raw(Ej, df::add_big_float((float)j, w.e)), {up.x, up.y});
         df::acc_fma(tail, df::div_raw(Ej, df::add_big_float((float)j, w.ome)), {dn.x, dn.y});
     }
+    // outer taps (j >= h_df, smallest first): weights E_j / (j + eps) small
+    // enough that FP32 products and sums stay far below the df error budget
+    float outer = 0.f;
+    for (int j = h - 1; j >= h_df; --j) {
+        const float Ej = edf[j - 1].hi;
+        outer = __fmaf_rn(Ej * df::rcp_approx((float)j + w.e.hi), y[d + 1 + j].x, outer);
+        outer = __fmaf_rn(Ej * df::rcp_approx((float)j + w.ome.hi), y[d - j].x, outer);
+    }
+    df::acc_add(tail, {outer, 0.f});
     df::acc_add(acc, df::mul(w.c, df::acc_value(tail)));
     return df::acc_value(acc);
 }
@@ -582,7 +591,8 @@ __device__ __forceinline__ void add_inner(double lk[6], const double *data, long
 // the three channels.
 __device__ __forceinline__ void df_interp_group(const float2 *y, const int off[3],
                                                 const float sg[3], int d, df::f2 A, df::f2 eps,
-                                                const df::f2 *edf, int h, df::f2 out[3]) {
+                                                const df::f2 *edf, int h, int h_df,
+                                                df::f2 out[3]) {
     const DfWeights w = df_weights(A, eps);
     df::Acc acc[3];
 #pragma unroll
@@ -596,11 +606,24 @@ __device__ __forceinline__ void df_interp_group(const float2 *y, const int off[3
     };
     tap(df::mul_raw(w.A, w.ome), d + 1);
     tap(df::mul_raw(w.A, w.e), d);
-    for (int j = 1; j < h; ++j) {
+    for (int j = 1; j < h_df; ++j) {
         const df::f2 cE = df::mul_raw(w.c, edf[j - 1]);  // unnormalised: mul_raw accepts it
         tap(df::div_raw(cE, df::add_big_float((float)j, w.e)), d + 1 + j);
         tap(df::div_raw(cE, df::add_big_float((float)j, w.ome)), d - j);
     }
+    // outer taps in FP32, smallest first (see df_interp_real)
+    float outer[3] = {0.f, 0.f, 0.f};
+    for (int j = h - 1; j >= h_df; --j) {
+        const float cE = w.c.hi * edf[j - 1].hi;
+        const float wu = cE * df::rcp_approx((float)j + w.e.hi);
+        const float wd = cE * df::rcp_approx((float)j + w.ome.hi);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            outer[c] = __fmaf_rn(wd, y[off[c] + d - j].x,
+                                 __fmaf_rn(wu, y[off[c] + d + 1 + j].x, outer[c]));
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) df::acc_add(acc[c], {outer[c], 0.f});
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const df::f2 v = df::acc_value(acc[c]);
@@ -1100,7 +1123,7 @@ __global__ void __launch_bounds__(kThreads, (kGrouped && !kDiag) ? 3 : 0)
                     }
                     const df::f2 A_df = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_df);
                     df::f2 val[3];
-                    df_interp_group(y32, off, sg, (int)(d - ya), A_df, e_df, edf, h, val);
+                    df_interp_group(y32, off, sg, (int)(d - ya), A_df, e_df, edf, h, a.h_df, val);
 #pragma unroll
                     for (int c = 0; c < 3; ++c) accdf[c] = df::add(accdf[c], val[c]);
                 }
@@ -1161,7 +1184,8 @@ __global__ void __launch_bounds__(kThreads, (kGrouped && !kDiag) ? 3 : 0)
                     }
                     if (kMixed) {
                         df::f2 val =
-                            df_interp_real(y32 + b * a.y_max, (int)(d - ya), A_df, e_df, edf, h);
+                            df_interp_real(y32 + b * a.y_max, (int)(d - ya), A_df, e_df, edf, h,
+                                           a.h_df);
                         const int sc = set->sign_code[unit];
                         if (sc == 1)
                             accdf[ch] = df::add(accdf[ch], val);

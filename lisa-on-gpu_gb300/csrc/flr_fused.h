@@ -97,6 +97,7 @@ struct FusedArgs {
     const FusedTdiSet *sets;
     int num_sets;
     const float4 *a_tab;       // per A-table knot: (A hi, A lo, dA hi, dA lo), dA = A[k+1]-A[k]
+    int h_df;                  // mixed TDI taps: j < h_df in double-float, the outer ones in FP32
     int tile;                  // output samples per work item
     int y_halo;                // link-stream samples computed before a tile
     int y_halo_hi;             // and after it: TDI delays only look back, so the taps

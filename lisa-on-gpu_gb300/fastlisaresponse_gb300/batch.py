@@ -206,10 +206,11 @@ class BatchedResponseTDI:
         _lib.check(rc)
         self._plan = plan
         self._graphs = {}
-        info = (ctypes.c_int * 8)()
-        lib.flr_batch_plan_info(plan, info, 8)
+        info = (ctypes.c_int * 9)()
+        lib.flr_batch_plan_info(plan, info, 9)
         self.plan_info = dict(zip(("tile", "y_halo", "win_max", "y_max", "smem_bytes",
-                                   "grid", "precision", "grouped"), list(info)))
+                                   "grid", "precision", "grouped", "fp32_tap_from"),
+                                  list(info)))
         self._ctor = dict(sampling_frequency=sampling_frequency, order=order, tdi=tdi,
                           orbits=orbits, tdi_chan=tdi_chan, precision=precision,
                           t_buffer=t_buffer, force_backend=self.device)

@@ -78,3 +78,19 @@ def test_largest_order(gpu_lib):
     with pytest.raises(ValueError):
         flr.BatchedResponseTDI(1 / dt, precision="mixed", order=81, tdi="2nd generation",
                                orbits=orb, t_buffer=2e4)
+
+
+def test_outer_taps_split(gpu_lib):
+    """The mixed kernel evaluates the outermost TDI taps in FP32 (weights below
+    5e-6 together): taps 10..12 at order 25, 14..22 at order 45; the fp64
+    flavour keeps every tap in FP64; the mixed channels stay within the bound
+    at both orders (test_largest_order and the batch tests cover the rest)."""
+    import fastlisaresponse_gb300 as flr
+
+    orb = flr.EqualArmlengthOrbits(t_max=1.2e6)
+    for order, first in ((25, 10), (45, 14)):
+        kw = dict(order=order, tdi="2nd generation", orbits=orb, t_buffer=2e4)
+        mx = flr.BatchedResponseTDI(0.1, precision="mixed", **kw)
+        fp = flr.BatchedResponseTDI(0.1, precision="fp64", **kw)
+        assert mx.plan_info["fp32_tap_from"] == first
+        assert fp.plan_info["fp32_tap_from"] == (order + 1) // 2
