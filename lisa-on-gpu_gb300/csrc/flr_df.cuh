@@ -98,9 +98,10 @@ __device__ __forceinline__ float rcp_approx(float x) {
     return r;
 }
 
-// 1 / b for b in [1, 64): hardware approximation refined by one Newton step
-// carried out on the df residual, r = r0 + r0 * (1 - b r0); relative error
-// about 1e-14.  Not normalised.
+// 1 / b for |b.hi| a normal float (the projection's 1 - k.n; 1/b must not
+// overflow): hardware approximation refined by one Newton step carried out on
+// the df residual, r = r0 + r0 * (1 - b r0); relative error about 1e-14.  Not
+// normalised.
 __device__ __forceinline__ f2 rcp(f2 b) {
     float r0 = rcp_approx(b.hi);
     float t = __fmaf_rn(-b.hi, r0, 1.0f);
