@@ -423,12 +423,13 @@ __device__ __forceinline__ DfWeights df_weights(df::f2 A, df::f2 e) {
     return w;
 }
 
-__device__ __forceinline__ df::f2 df_tail_up(const DfWeights &w, df::f2 Ej, int j) {
-    return df::div_raw(df::mul_raw(w.c, Ej), df::add_big_float((float)j, w.e));
+// j: the tap's distance as a float (exact)
+__device__ __forceinline__ df::f2 df_tail_up(const DfWeights &w, df::f2 Ej, float j) {
+    return df::div_raw(df::mul_raw(w.c, Ej), df::add_big_float(j, w.e));
 }
 
-__device__ __forceinline__ df::f2 df_tail_dn(const DfWeights &w, df::f2 Ej, int j) {
-    return df::div_raw(df::mul_raw(w.c, Ej), df::add_big_float((float)j, w.ome));
+__device__ __forceinline__ df::f2 df_tail_dn(const DfWeights &w, df::f2 Ej, float j) {
+    return df::div_raw(df::mul_raw(w.c, Ej), df::add_big_float(j, w.ome));
 }
 
 // Shared-memory df views of the staged input: value and first difference.
@@ -476,7 +477,12 @@ __device__ __forceinline__ void df_interp_c128_sbp(const Src &src, typename Src:
         df::acc_fma(sre, P, {dx.x, dx.y});
         df::acc_fma(sim, P, {dx.z, dx.w});
     };
-    for (int j = h - 1; j >= 1; --j) step(df_tail_dn(w, edf[j - 1], j), d - j);
+    {  // taps d - (h - 1) .. d - 1, j = h - 1 .. 1
+        const df::f2 *Ej = edf + h - 2;
+        float jf = (float)(h - 1);
+        for (index_t k = d - (h - 1); k < d; ++k, --Ej, jf -= 1.f)
+            step(df_tail_dn(w, *Ej, jf), k);
+    }
     step(df::mul_raw(w.A, w.e), d);
     df::f2 W_last;
     index_t last;
@@ -485,8 +491,10 @@ __device__ __forceinline__ void df_interp_c128_sbp(const Src &src, typename Src:
         last = d + 1;
     } else {
         step(df::mul_raw(w.A, w.ome), d + 1);
-        for (int j = 1; j < h - 1; ++j) step(df_tail_up(w, edf[j - 1], j), d + 1 + j);
-        W_last = df_tail_up(w, edf[h - 2], h - 1);
+        const df::f2 *Ej = edf;  // taps d + 2 .. d + h - 1, j = 1 .. h - 2
+        float jf = 1.f;
+        for (index_t k = d + 2; k < d + h; ++k, ++Ej, jf += 1.f) step(df_tail_up(w, *Ej, jf), k);
+        W_last = df_tail_up(w, edf[h - 2], (float)(h - 1));
         last = d + h;
     }
     P = df::add(P, W_last);
@@ -529,19 +537,26 @@ __device__ __forceinline__ df::f2 df_interp_real(const float2 *y, int d, df::f2 
     df::acc_fma(acc, df::mul_raw(w.A, w.ome), {v.x, v.y});
     v = y[d];
     df::acc_fma(acc, df::mul_raw(w.A, w.e), {v.x, v.y});
-    for (int j = 1; j < h_df; ++j) {
-        const df::f2 Ej = edf[j - 1];
-        float2 up = y[d + 1 + j], dn = y[d - j];
-        df::acc_fma(tail, df::div_raw(Ej, df::add_big_float((float)j, w.e)), {up.x, up.y});
-        df::acc_fma(tail, df::div_raw(Ej, df::add_big_float((float)j, w.ome)), {dn.x, dn.y});
+    // taps j = 1 .. h_df - 1 at y[d + 1 + j] and y[d - j]; running pointers and
+    // a float copy of j (exact) keep the loop free of index arithmetic
+    const float2 *up = y + d + 2, *dn = y + d - 1;
+    const df::f2 *Ej = edf;
+    float jf = 1.f;
+    for (int j = 1; j < h_df; ++j, ++up, --dn, ++Ej, jf += 1.f) {
+        const float2 u = *up, v = *dn;
+        df::acc_fma(tail, df::div_raw(*Ej, df::add_big_float(jf, w.e)), {u.x, u.y});
+        df::acc_fma(tail, df::div_raw(*Ej, df::add_big_float(jf, w.ome)), {v.x, v.y});
     }
     // outer taps (j >= h_df, smallest first): weights E_j / (j + eps) small
     // enough that FP32 products and sums stay far below the df error budget
     float outer = 0.f;
-    for (int j = h - 1; j >= h_df; --j) {
-        const float Ej = edf[j - 1].hi;
-        outer = __fmaf_rn(Ej * df::rcp_approx((float)j + w.e.hi), y[d + 1 + j].x, outer);
-        outer = __fmaf_rn(Ej * df::rcp_approx((float)j + w.ome.hi), y[d - j].x, outer);
+    up = y + d + h;
+    dn = y + d + 1 - h;
+    Ej = edf + h - 2;
+    jf = (float)(h - 1);
+    for (int j = h - 1; j >= h_df; --j, --up, ++dn, --Ej, jf -= 1.f) {
+        outer = __fmaf_rn(Ej->hi * df::rcp_approx(jf + w.e.hi), up->x, outer);
+        outer = __fmaf_rn(Ej->hi * df::rcp_approx(jf + w.ome.hi), dn->x, outer);
     }
     df::acc_add(tail, {outer, 0.f});
     df::acc_add(acc, df::mul(w.c, df::acc_value(tail)));
@@ -606,10 +621,12 @@ __device__ __forceinline__ void df_interp_group(const float2 *y, const int off[3
     };
     tap(df::mul_raw(w.A, w.ome), d + 1);
     tap(df::mul_raw(w.A, w.e), d);
-    for (int j = 1; j < h_df; ++j) {
-        const df::f2 cE = df::mul_raw(w.c, edf[j - 1]);  // unnormalised: mul_raw accepts it
-        tap(df::div_raw(cE, df::add_big_float((float)j, w.e)), d + 1 + j);
-        tap(df::div_raw(cE, df::add_big_float((float)j, w.ome)), d - j);
+    const df::f2 *Ej = edf;
+    float jf = 1.f;  // j as a float (exact)
+    for (int j = 1; j < h_df; ++j, ++Ej, jf += 1.f) {
+        const df::f2 cE = df::mul_raw(w.c, *Ej);  // unnormalised: mul_raw accepts it
+        tap(df::div_raw(cE, df::add_big_float(jf, w.e)), d + 1 + j);
+        tap(df::div_raw(cE, df::add_big_float(jf, w.ome)), d - j);
     }
     // outer taps in FP32, smallest first (see df_interp_real)
     float outer[3] = {0.f, 0.f, 0.f};
