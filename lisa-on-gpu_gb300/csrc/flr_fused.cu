@@ -609,35 +609,40 @@ __device__ __forceinline__ void df_interp_group(const float2 *y, const int off[3
                                                 const df::f2 *edf, int h, int h_df,
                                                 df::f2 out[3]) {
     const DfWeights w = df_weights(A, eps);
+    // per channel: its virtual row around sample d; taps at row[k], k relative to d
+    const float2 *row[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) row[c] = y + off[c] + d;
     df::Acc acc[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) df::acc_init(acc[c]);
     auto tap = [&](df::f2 W, int k) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const float2 v = y[off[c] + k];
+            const float2 v = row[c][k];
             df::acc_fma(acc[c], W, {v.x, v.y});
         }
     };
-    tap(df::mul_raw(w.A, w.ome), d + 1);
-    tap(df::mul_raw(w.A, w.e), d);
+    tap(df::mul_raw(w.A, w.ome), 1);
+    tap(df::mul_raw(w.A, w.e), 0);
     const df::f2 *Ej = edf;
     float jf = 1.f;  // j as a float (exact)
     for (int j = 1; j < h_df; ++j, ++Ej, jf += 1.f) {
         const df::f2 cE = df::mul_raw(w.c, *Ej);  // unnormalised: mul_raw accepts it
-        tap(df::div_raw(cE, df::add_big_float(jf, w.e)), d + 1 + j);
-        tap(df::div_raw(cE, df::add_big_float(jf, w.ome)), d - j);
+        tap(df::div_raw(cE, df::add_big_float(jf, w.e)), 1 + j);
+        tap(df::div_raw(cE, df::add_big_float(jf, w.ome)), -j);
     }
     // outer taps in FP32, smallest first (see df_interp_real)
     float outer[3] = {0.f, 0.f, 0.f};
-    for (int j = h - 1; j >= h_df; --j) {
-        const float cE = w.c.hi * edf[j - 1].hi;
-        const float wu = cE * df::rcp_approx((float)j + w.e.hi);
-        const float wd = cE * df::rcp_approx((float)j + w.ome.hi);
+    jf = (float)(h - 1);
+    Ej = edf + h - 2;
+    for (int j = h - 1; j >= h_df; --j, --Ej, jf -= 1.f) {
+        const float cE = w.c.hi * Ej->hi;
+        const float wu = cE * df::rcp_approx(jf + w.e.hi);
+        const float wd = cE * df::rcp_approx(jf + w.ome.hi);
 #pragma unroll
         for (int c = 0; c < 3; ++c)
-            outer[c] = __fmaf_rn(wd, y[off[c] + d - j].x,
-                                 __fmaf_rn(wu, y[off[c] + d + 1 + j].x, outer[c]));
+            outer[c] = __fmaf_rn(wd, row[c][-j].x, __fmaf_rn(wu, row[c][1 + j].x, outer[c]));
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) df::acc_add(acc[c], {outer[c], 0.f});
