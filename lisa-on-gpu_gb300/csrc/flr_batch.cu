@@ -563,7 +563,7 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
         b.rx_sc[r] = r + 1;
         if (found != 2) b.rx_shared = 0;
     }
-    b.trio = b.rx_shared;
+    b.trio = b.rx_shared && equal_arms;
     for (int r = 0; r < 3; ++r) {
         b.tx_slot[r] = -1;
         for (int slot = 5; slot >= 0; --slot)

@@ -301,15 +301,13 @@ struct EmitterF64 {
     double xi_p, xi_c, k_dot_n;
 };
 
-__device__ __forceinline__ EmitterF64 emitter_f64(const OrbitTables &o, int slot, double t,
-                                                  const double x_rec[3], double t_first,
-                                                  double fs, const double k[3],
-                                                  const double u[3], const double v[3]) {
-    EmitterF64 e;
-    const double L = light_travel_time(o, t, slot);
-    const double t_em = t - L;
-    double x_em[3], n[3];
-    position(o, t_em, o.sc_e[slot], x_em);
+// Polarisation projections and k.n of one link, n = (x_rec - x_em)/|x_rec - x_em|
+// (link_geometry()'s operations in its order).
+__device__ __forceinline__ void link_projection_f64(const double x_rec[3], const double x_em[3],
+                                                    const double k[3], const double u[3],
+                                                    const double v[3], double &xi_p,
+                                                    double &xi_c, double &k_dot_n) {
+    double n[3];
     double norm = 0.0;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -320,12 +318,32 @@ __device__ __forceinline__ EmitterF64 emitter_f64(const OrbitTables &o, int slot
 #pragma unroll
     for (int c = 0; c < 3; ++c) n[c] = n[c] / norm;
     const double un = dot3(u, n), vn = dot3(v, n);
-    e.xi_p = 0.5 * ((un * un) - (vn * vn));
-    e.xi_c = un * vn;
-    e.k_dot_n = dot3(k, n);
+    xi_p = 0.5 * ((un * un) - (vn * vn));
+    xi_c = un * vn;
+    k_dot_n = dot3(k, n);
+}
+
+// Emission time, position and index split of spacecraft sc's side of a link
+// with light travel time L (the emitter half of link_geometry()).
+__device__ __forceinline__ void emitter_side_f64(const OrbitTables &o, int sc, double t, double L,
+                                                 double t_first, double fs, const double k[3],
+                                                 double x_em[3], int &d_em, double &e_em) {
+    const double t_em = t - L;
+    position(o, t_em, sc, x_em);
     const double kx_em = dot3(k, x_em);
     const double delay_em = t_em - kx_em * kCInv;
-    split_delay(delay_em, t_first, fs, e.d_em, e.e_em);
+    split_delay(delay_em, t_first, fs, d_em, e_em);
+}
+
+__device__ __forceinline__ EmitterF64 emitter_f64(const OrbitTables &o, int slot, double t,
+                                                  const double x_rec[3], double t_first,
+                                                  double fs, const double k[3],
+                                                  const double u[3], const double v[3]) {
+    EmitterF64 e;
+    double x_em[3];
+    emitter_side_f64(o, o.sc_e[slot], t, light_travel_time(o, t, slot), t_first, fs, k, x_em,
+                     e.d_em, e.e_em);
+    link_projection_f64(x_rec, x_em, k, u, v, e.xi_p, e.xi_c, e.k_dot_n);
     return e;
 }
 
@@ -949,6 +967,79 @@ __global__ void __launch_bounds__(kThreads, (kGrouped && !kDiag) ? 3 : 0)
                     y32[slot * a.y_max + jj] = make_float2(yv.hi, yv.lo);
                     if (kDiag && own && src.y_out)
                         src.y_out[(long)slot * n + j] = df::to_double(yv) / scale;
+                }
+            }
+        } else if (!kMixed && a.trio) {
+            // exact flavour on equal arms: three lanes per sample as in the
+            // mixed form; lane r computes spacecraft r + 1's receiver side and
+            // the emitter side that every link leaving it shares (the same
+            // L(t) bits on every link, hence the same t_em, position, split and
+            // interpolation), and each link's projection from its two sides:
+            // the per-link form's operations, 6 interpolations instead of 9
+            const int lane = tid & 31, sub = lane / 3, r = lane - 3 * sub;
+            const int rr = (r < 3) ? r : 0;
+            for (int base = (tid >> 5) * 10; base < Y; base += 10 * (kThreads / 32)) {
+                const int jj = base + sub;
+                const bool act = (sub < 10) && (jj < Y);
+                const long j = ya + jj;
+                const bool live = act && j >= yfirst && j < ylast;
+                const double t = t0 + (double)j * a.dt;
+                ReceiverF64 rs{};
+                double x_em[3] = {0.0, 0.0, 0.0};
+                int d_em = 0;
+                double hp_r = 0.0, hc_r = 0.0, hp_e = 0.0, hc_e = 0.0;
+                bool okA_r = false, okT_r = false, okA_e = false, okT_e = false;
+                if (live) {
+                    rs = receiver_f64(a.orb, rr + 1, t, t0, a.fs, k);
+                    double A_r;
+                    okA_r = prefactor(a.lt, rs.e_rec, A_r);
+                    okT_r = okA_r && c128_any(hraw, wlo, W, src.h, n, rs.d_rec, rs.e_rec, A_r,
+                                              a.lt, hp_r, hc_r);
+                    double e_em, A_e;
+                    emitter_side_f64(a.orb, rr + 1, t, light_travel_time(a.orb, t, a.tx_slot[rr]),
+                                     t0, a.fs, k, x_em, d_em, e_em);
+                    okA_e = prefactor(a.lt, e_em, A_e);
+                    okT_e = okA_e && c128_any(hraw, wlo, W, src.h, n, d_em, e_em, A_e, a.lt,
+                                              hp_e, hc_e);
+                }
+                const bool own = live && (j >= o0 && j < o1);  // diagnostics
+                for (int q = 0; q < 2; ++q) {
+                    const int slot = a.rx_slot[rr][q];
+                    const int from = min(3 * sub + a.orb.sc_e[slot] - 1, 31);
+                    const unsigned full = 0xffffffffu;
+                    const double xhp = __shfl_sync(full, hp_e, from);
+                    const double xhc = __shfl_sync(full, hc_e, from);
+                    const bool xokA = __shfl_sync(full, (int)okA_e, from) != 0;
+                    const bool xokT = __shfl_sync(full, (int)okT_e, from) != 0;
+                    double xem[3];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) xem[c] = __shfl_sync(full, x_em[c], from);
+                    const int xd_em = __shfl_sync(full, d_em, from);
+                    if (!act) continue;
+                    if (!live) {  // the reference's y_gw is zero there
+                        y64[slot * a.y_max + jj] = 0.0;
+                        continue;
+                    }
+                    if (kDiag && own && src.d_rec_out) {
+                        src.d_rec_out[(long)slot * n + j] = rs.d_rec;
+                        src.d_em_out[(long)slot * n + j] = xd_em;
+                    }
+                    double out;
+                    if (!(okA_r && xokA)) {
+                        raise_status(a.orb.status, kStatusAIndex);
+                        out = qnan();
+                    } else if (okT_r && xokT) {
+                        double xi_p, xi_c, k_dot_n;
+                        link_projection_f64(rs.x_rec, xem, k, u, v, xi_p, xi_c, k_dot_n);
+                        double pre = 1. / (1. - k_dot_n);
+                        double big = (xhp - hp_r) * xi_p + (xhc - hc_r) * xi_c;
+                        out = pre * big;
+                    } else {
+                        raise_status(a.orb.status, kStatusTap);
+                        out = qnan();
+                    }
+                    y64[slot * a.y_max + jj] = out;
+                    if (kDiag && own && src.y_out) src.y_out[(long)slot * n + j] = out;
                 }
             }
         } else if (!kMixed && a.rx_shared) {

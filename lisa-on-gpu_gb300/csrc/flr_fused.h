@@ -114,8 +114,9 @@ struct FusedArgs {
     int rx_shared;
     int rx_sc[3];
     int rx_slot[3][2];
-    // tx_slot[r]: a link spacecraft r + 1 emits on (trio = 1 when all three
-    // emit; with equal arms all links leaving a spacecraft share t_em)
+    // tx_slot[r]: a link spacecraft r + 1 emits on; trio = 1 when all three
+    // emit and the six arms are equal at every orbit knot, so that all links
+    // leaving a spacecraft share t_em (bit for bit)
     int trio;
     int tx_slot[3];
 };
