@@ -7,10 +7,14 @@
 //      of the stream range), and stages it into shared memory with one 1-D
 //      bulk copy (cp.async.bulk, mbarrier completion, bounded wait);
 //   2. computes the six link streams y for [o0 - halo, o1 + halo) into shared
-//      memory (one (link, sample) per thread iteration);
+//      memory: one (receiving spacecraft, sample) per thread iteration, or,
+//      on equal arms, three lanes per sample sharing the emitter sides by
+//      warp shuffles (one (link, sample) per iteration for other link tables);
 //   3. computes the TDI channels of [o0, o1) from those streams (one output
-//      sample, all units of all channels, per thread iteration) and writes
-//      X/Y/Z (or A/E/T, A/E) to global memory.
+//      sample, all units of all channels, per thread iteration; in the mixed
+//      flavour on equal arms, units of equal delay evaluated as groups over
+//      signed link-row combinations) and writes X/Y/Z (or A/E/T, A/E) to
+//      global memory.
 // The link streams never touch HBM: per output sample the kernel reads 16 B
 // of input and writes 24 B (plus the halos).
 //
