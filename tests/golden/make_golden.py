@@ -60,6 +60,11 @@ CASES = {
                                 tdi="2nd generation", chan="AE", t0=0.0,
                                 wave=("config", 1e-23, 1e-4, 1e-18, 1.4, 0.6, 0.3), lam=2.9,
                                 beta=-0.1),
+    # the highest order the reference's factorial table supports (39!)
+    "flex_gen2_o39": dict(orbits="kepler", dt=10.0, n=4096, order=39, tdi="2nd generation",
+                          chan="XYZ", t0=5.0e4,
+                          wave=("config", 3e-22, 1e-3, 1e-15, 0.9, 2.2, 1.0), lam=3.3,
+                          beta=0.2),
 }
 
 
@@ -106,8 +111,11 @@ def run_case(name: str, c: dict) -> dict:
     )
 
 
-def main():
+def main(names=None):
+    """Write every case, or only the named ones (python make_golden.py NAME ...)."""
     for name, c in CASES.items():
+        if names and name not in names:
+            continue
         out = run_case(name, c)
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **out)
@@ -116,4 +124,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])
