@@ -1,8 +1,8 @@
 // Arithmetic-pipe throughput probes (diagnostics).
 //
 // The response + TDI kernels are bound by the FP64 pipe, whose peak is not in
-// the driver's measured-peak table (it lists HBM bandwidth and bf16 tensor
-// throughput).  These kernels measure it the same way those peaks were
+// the measured-peak table of the machine (it lists HBM bandwidth and bf16
+// tensor throughput).  These kernels measure it the same way those peaks are
 // measured -- a saturating loop timed with CUDA events -- so the roofline
 // fraction of the response kernels has a measured denominator.
 //

@@ -15,8 +15,8 @@
  * and the orbit-table evaluation of lisaanalysistools' Orbits class (restated;
  * that source is absent, see oracle/ref_shim/Detector.hpp for the rules).
  *
- * Pinned bit-for-bit against the reference's own CPU code compiled from
- * /root/reference with the shim headers (oracle/Makefile, target `ref`) and
+ * Pinned bit-for-bit against the reference's own CPU code compiled from the
+ * reference checkout with the shim headers (oracle/Makefile, target `ref`) and
  * against golden fixtures generated by driving the reference's Python layer
  * (tests/golden/make_golden.py).
  */
