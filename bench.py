@@ -203,11 +203,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sms)}
 
 
-def measure_fp64_peak(lib, device) -> dict:
-    """FP64 FMA and FP32 FMA rates of this GPU from the probe kernel (best of 3)."""
+def measure_fp64_peak(device) -> dict:
+    """FP64 FMA, FP64 division and FP32 FMA rates of this GPU from the probe
+    kernels of libflr_probe.so (best of 3)."""
     import ctypes
 
     import torch
+
+    from fastlisaresponse_gb300 import _build
+
+    lib = ctypes.CDLL(_build.PROBE_LIB_PATH)
+    lib.flr_probe_pipe_rate.restype = ctypes.c_int
+    lib.flr_probe_pipe_rate.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_void_p, ctypes.POINTER(ctypes.c_float),
+                                        ctypes.c_void_p]
 
     sms = torch.cuda.get_device_properties(device).multi_processor_count
     blocks, threads = sms * 8, 256
@@ -604,7 +613,7 @@ def run_ours(args, rank, world, device):
     n_out = output_samples(n, dt)
     h_dev = torch.as_tensor(h, device=device)
     lib = _lib.lib()
-    peaks = measure_fp64_peak(lib, device)
+    peaks = measure_fp64_peak(device)
 
     def barrier():
         if world > 1:

@@ -331,15 +331,6 @@ int flr_get_response_noalloc(double orbit_dt, int orbit_N, const double *ltt_arr
                              const double *A_in, double deps, int num_A, const double *E_in,
                              int projections_start_ind, void *stream);
 
-/*
- * Diagnostics: arithmetic-pipe throughput probe (no reference counterpart).
- * Runs blocks x threads threads, each `iters` iterations of 8 independent
- * operations of `kind` (0 = FP64 FMA, 1 = FP64 division, 2 = FP32 FMA), timed
- * with CUDA events on `stream`; synchronises.  Used as the measured FP64-pipe
- * peak of the roofline.  `sink` is a device buffer of `blocks` doubles.
- */
-int flr_probe_pipe_rate(int kind, long iters, int blocks, int threads, double *sink,
-                        float *elapsed_ms, void *stream);
 
 #ifdef __cplusplus
 }

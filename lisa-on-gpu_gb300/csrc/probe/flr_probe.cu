@@ -1,4 +1,5 @@
-// Arithmetic-pipe throughput probes (diagnostics).
+// Arithmetic-pipe throughput probes of the benchmark (libflr_probe.so, not the
+// product library).
 //
 // The response + TDI kernels are bound by the FP64 pipe, whose peak is not in
 // the measured-peak table of the machine (it lists HBM bandwidth and bf16
@@ -15,7 +16,7 @@
 // iters * 8.
 #include <cuda_runtime.h>
 
-#include "../../include/flr_gb300.h"
+#include "flr_probe.h"
 
 namespace {
 
@@ -67,13 +68,13 @@ extern "C" int flr_probe_pipe_rate(int kind, long iters, int blocks, int threads
                                    float *elapsed_ms, void *stream) {
     if (kind < 0 || kind > 2 || iters < 1 || blocks < 1 || threads < 32 || threads > 1024 ||
         !sink || !elapsed_ms)
-        return FLR_E_INVALID_ARGUMENT;
+        return -1;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaEvent_t e0, e1;
-    if (cudaEventCreate(&e0) != cudaSuccess) return FLR_E_CUDA;
+    if (cudaEventCreate(&e0) != cudaSuccess) return -2;
     if (cudaEventCreate(&e1) != cudaSuccess) {
         cudaEventDestroy(e0);
-        return FLR_E_CUDA;
+        return -2;
     }
     cudaEventRecord(e0, s);
     if (kind == 0)
@@ -88,5 +89,5 @@ extern "C" int flr_probe_pipe_rate(int kind, long iters, int blocks, int threads
     if (err == cudaSuccess) err = cudaEventElapsedTime(elapsed_ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    return err == cudaSuccess ? FLR_OK : FLR_E_CUDA;
+    return err == cudaSuccess ? 0 : -2;
 }

@@ -21,6 +21,9 @@ INCLUDE = os.path.normpath(os.path.join(PKG_DIR, "..", "..", "include"))
 LIB_DIR = os.path.join(PKG_DIR, "_lib")
 OBJ_DIR = os.path.join(LIB_DIR, "obj")
 LIB_PATH = os.path.join(LIB_DIR, "libflr_gb300.so")
+# the benchmark's arithmetic-pipe probe: a library of its own, not the product's
+PROBE_SRC = os.path.join(CSRC, "probe", "flr_probe.cu")
+PROBE_LIB_PATH = os.path.join(LIB_DIR, "libflr_probe.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INCLUDE]
@@ -29,7 +32,6 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", CSRC, "
 SOURCES = {
     "flr_plain.cu": ["--fmad=false"],
     "flr_capi.cu": [],
-    "flr_probe.cu": [],
     "flr_noalloc.cu": ["--fmad=false"],
     "flr_fused.cu": ["--fmad=false"],
     "flr_batch.cu": [],
@@ -49,14 +51,15 @@ def _nvcc() -> str:
 def _inputs() -> list:
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)
              if f.endswith((".cu", ".cuh", ".h"))]
+    files += [PROBE_SRC, os.path.join(CSRC, "probe", "flr_probe.h")]
     files += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     return files
 
 
 def needs_build() -> bool:
-    if not os.path.exists(LIB_PATH):
+    if not os.path.exists(LIB_PATH) or not os.path.exists(PROBE_LIB_PATH):
         return True
-    built = os.path.getmtime(LIB_PATH)
+    built = min(os.path.getmtime(LIB_PATH), os.path.getmtime(PROBE_LIB_PATH))
     return any(os.path.getmtime(f) > built for f in _inputs()) or \
         os.path.getmtime(__file__) > built
 
@@ -82,8 +85,18 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 print(res.stdout + res.stderr)
             return obj
 
-        with ThreadPoolExecutor(max_workers=len(SOURCES)) as pool:
+        def build_probe():
+            tmp = PROBE_LIB_PATH + ".tmp"
+            cmd = [nvcc, *ARCH, *COMMON, "-shared", PROBE_SRC, "-o", tmp]
+            res = subprocess.run(cmd, capture_output=True, text=True)
+            if res.returncode != 0:
+                raise RuntimeError(f"nvcc failed on the probe:\n{res.stdout}\n{res.stderr}")
+            os.replace(tmp, PROBE_LIB_PATH)
+
+        with ThreadPoolExecutor(max_workers=len(SOURCES) + 1) as pool:
+            probe = pool.submit(build_probe)
             objs = list(pool.map(compile_one, SOURCES.items()))
+            probe.result()
         tmp = LIB_PATH + ".tmp"
         cmd = [nvcc, *ARCH, "-shared", *objs, "-o", tmp]
         res = subprocess.run(cmd, capture_output=True, text=True)

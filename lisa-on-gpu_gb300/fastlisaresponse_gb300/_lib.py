@@ -48,8 +48,6 @@ _SIGNATURES = {
                                 _i, _p, _d, _i, _p, _i, _p]),
     "flr_response_delay_indices": (_i, [_p, _p, _p, _p, _p, _i, _d, _i, _p]),
     "flr_tdi_delay_indices": (_i, [_p, _p, _i, _p, _p, _p, _p, _i, _d, _i, _p]),
-    "flr_probe_pipe_rate": (_i, [_i, ctypes.c_long, _i, _i, _p, ctypes.POINTER(ctypes.c_float),
-                                 _p]),
 }
 
 

@@ -32,7 +32,23 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("FLR_REFERENCE_ROOT", "/root/reference")
+
+
+def _reference_root() -> str:
+    """The reference checkout: FLR_REFERENCE_ROOT, else the location the
+    oracle's Makefile (the recipe that compiles the checkout) names."""
+    env = os.environ.get("FLR_REFERENCE_ROOT")
+    if env:
+        return env
+    try:
+        res = subprocess.run(["make", "-s", "-C", HERE, "print-ref-root"], capture_output=True,
+                             text=True, check=True)
+        return res.stdout.strip()
+    except (OSError, subprocess.CalledProcessError):
+        return ""
+
+
+REF_ROOT = _reference_root()
 REF_PKG = os.path.join(REF_ROOT, "src", "fastlisaresponse")
 REF_LIB = os.path.join(HERE, "_ref", "libflr_ref.so")
 

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this folder from the reference's own code.
 
-Run where the reference checkout exists (it is read from FLR_REFERENCE_ROOT,
-default /root/reference):
+Run where the reference checkout exists (FLR_REFERENCE_ROOT, or the location
+``oracle/Makefile`` names):
 
     python tests/golden/make_golden.py
 

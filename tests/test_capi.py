@@ -74,3 +74,12 @@ def test_no_oracle_in_the_product():
                 text = open(os.path.join(dirpath, f)).read()
                 assert "import oracle" not in text and "from oracle" not in text, f
                 assert "refdrive" not in text, f
+
+
+def test_probe_is_not_in_the_product_library(lib):
+    """The benchmark's pipe probe is built into its own library."""
+    from fastlisaresponse_gb300 import _build
+
+    assert not hasattr(lib, "flr_probe_pipe_rate")
+    probe = ctypes.CDLL(_build.PROBE_LIB_PATH)
+    assert hasattr(probe, "flr_probe_pipe_rate")
