@@ -315,7 +315,9 @@ int flr_batch_graph_destroy(flr_batch_graph *graph);
  *   links, sc_r, sc_e [6]   HOST arrays (read during the call)
  * The derived segment slopes and the status word live in a fixed array inside
  * the library (3.9 MB of device memory on every GPU that loads it, held until
- * exit), rewritten and cleared by every call.  The first call on a device,
+ * exit), rewritten and cleared by every call; out-of-range tap windows set
+ * FLR_STATUS_* bits there (flr_noalloc_status reads them) and give NaN, as in
+ * flr_get_response.  The first call on a device,
  * with that device current, looks up the array's device address; make it
  * before any stream capture.  Calls whose work can overlap on the GPU race on
  * the array.  Sizes beyond the limit return FLR_E_INVALID_ARGUMENT with the
@@ -330,6 +332,16 @@ int flr_get_response_noalloc(double orbit_dt, int orbit_N, const double *ltt_arr
                              int order, double sampling_frequency, int buffer_integer,
                              const double *A_in, double deps, int num_A, const double *E_in,
                              int projections_start_ind, void *stream);
+
+/*
+ * Status word of the allocation-free entry point (FLR_STATUS_* bits, as
+ * flr_orbits_status reports them for a handle), read from the same fixed
+ * array without allocating; reset != 0 also clears it.  Every call of
+ * flr_get_response_noalloc clears the word first, so it describes the latest
+ * call on this device only.  Synchronises `stream`.  No counterpart in the
+ * reference.
+ */
+int flr_noalloc_status(uint32_t *bits, int reset, void *stream);
 
 
 #ifdef __cplusplus

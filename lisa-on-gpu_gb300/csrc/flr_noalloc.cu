@@ -23,6 +23,11 @@
 // work overlaps on the GPU (different streams, no ordering between them)
 // race on it.  Results of a call are identical, bit for bit, to
 // flr_get_response with the same tables.
+//
+// The kernel's status bits (an interpolation window that leaves the input, an
+// A-table index out of range) land in the array's status word, which the next
+// call clears: flr_noalloc_status() reads it (and optionally clears it)
+// without allocating, so it holds the result of the latest call only.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -44,6 +49,8 @@ std::mutex g_lock;
 double *g_scratch_ptr[kMaxDevices] = {nullptr};
 
 int noalloc_fail(int code, const std::string &msg) {
+    // a handled CUDA error must not resurface in a later, unrelated check
+    if (code == FLR_E_CUDA) cudaGetLastError();
     flr::set_last_error(msg);
     return code;
 }
@@ -157,5 +164,26 @@ extern "C" int flr_get_response_noalloc(double orbit_dt, int orbit_N, const doub
     if (err != cudaSuccess)
         return noalloc_fail(FLR_E_CUDA, std::string("launching the response kernel: ") +
                                             cudaGetErrorString(err));
+    return FLR_OK;
+}
+
+extern "C" int flr_noalloc_status(uint32_t *bits, int reset, void *stream) {
+    flr::set_last_error("");
+    if (!bits) return noalloc_fail(FLR_E_INVALID_ARGUMENT, "bits must not be NULL");
+    double *scratch = nullptr;
+    cudaError_t err = scratch_address(&scratch);
+    if (err != cudaSuccess)
+        return noalloc_fail(FLR_E_CUDA, std::string("cudaGetSymbolAddress: ") +
+                                            cudaGetErrorString(err));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned *word = reinterpret_cast<unsigned *>(scratch + kSlopeDoubles);
+    unsigned value = 0u;
+    err = cudaMemcpyAsync(&value, word, sizeof(value), cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess && reset) err = cudaMemsetAsync(word, 0, sizeof(unsigned), s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    if (err != cudaSuccess)
+        return noalloc_fail(FLR_E_CUDA, std::string("reading the status word: ") +
+                                            cudaGetErrorString(err));
+    *bits = value;
     return FLR_OK;
 }
