@@ -60,6 +60,15 @@ extern "C" {
 #define FLR_STATUS_A_INDEX_OUT_OF_RANGE 0x2u /* eps/deps outside the A table        */
 #define FLR_STATUS_BAD_LINK 0x4u           /* link number not in the orbit's links  */
 #define FLR_STATUS_BAD_CHANNEL 0x8u        /* TDI channel outside [0,num_channels)  */
+/* Batched kernel only: a work item's staging copy did not complete within its
+ * first wait; it completed within a second one and that item's outputs are
+ * NaN (the batch's other outputs are valid). */
+#define FLR_STATUS_STAGING 0x10u
+/* Batched kernel only: a staging copy did not complete within the second wait
+ * either; the block that issued it left the launch with the copy in flight,
+ * so every output of the launches since the status was last cleared is to be
+ * discarded (flr_orbits_status also says so in flr_last_error()). */
+#define FLR_STATUS_STAGING_LOST 0x20u
 
 /* Largest Lagrange order accepted (h = (order+1)/2 <= 40, the reference's
  * MAX_ORDER E-table size, LISAResponse.cu:216). */
@@ -260,6 +269,14 @@ int flr_batch_plan_destroy(flr_batch_plan *plan);
  * that the mixed kernel evaluates in FP32 (its weights are small enough; the
  * half-width h when none). */
 int flr_batch_plan_info(const flr_batch_plan *plan, int *info, int n_info);
+
+/* Test hook (no reference counterpart): the bound, in mbarrier polls, of each
+ * work item's first wait for its staging copy in the plan's later runs and
+ * graphs (polls < 0 restores the default, 2^20).  With 0 every first wait
+ * gives up at once, so the give-up path runs without a stalled copy: a second
+ * wait with the full bound lets the copy land, the item's outputs become NaN
+ * and FLR_STATUS_STAGING is raised. */
+int flr_batch_plan_set_wait_limit(flr_batch_plan *plan, long long polls);
 
 /* Evaluate `num_sources` sources (host array of descriptors) on `stream`. */
 int flr_batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int num_sources,

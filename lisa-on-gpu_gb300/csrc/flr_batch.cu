@@ -547,6 +547,7 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
                                                        set_off);
     b.num_sets = num_sets;
     b.a_tab = reinterpret_cast<const float4 *>(static_cast<char *>(p->d_tables) + atab_off);
+    b.wait_polls = flr::kFusedWaitPolls;
     b.fs = sampling_frequency;
     b.dt = 1.0 / sampling_frequency;
     b.inv_deps = 1.0 / deps;
@@ -589,6 +590,14 @@ int flr_batch_plan_info(const flr_batch_plan *plan, int *info, int n_info) {
                         plan->mixed ? FLR_PRECISION_MIXED : FLR_PRECISION_FP64,
                         plan->grouped ? 1 : 0, plan->base.h_df};
     for (int i = 0; i < n_info && i < (int)(sizeof(vals) / sizeof(int)); ++i) info[i] = vals[i];
+    return FLR_OK;
+}
+
+int flr_batch_plan_set_wait_limit(flr_batch_plan *plan, long long polls) {
+    flr::set_last_error("");
+    if (!plan) return fail(FLR_E_INVALID_ARGUMENT, "plan must not be NULL");
+    plan->base.wait_polls = (polls < 0) ? flr::kFusedWaitPolls
+                                        : (long)std::min<long long>(polls, flr::kFusedWaitPolls);
     return FLR_OK;
 }
 

@@ -178,6 +178,12 @@ int flr_orbits_status(flr_orbits *orbits, uint32_t *bits, int reset, void *strea
     if (err == cudaSuccess) err = cudaStreamSynchronize(s);
     if (err != cudaSuccess) return cuda_fail(err, "reading the status word");
     *bits = host;
+    if (host & FLR_STATUS_STAGING_LOST)
+        g_last_error = "a staging copy of the batched kernel never completed: discard every "
+                       "output of the batches run since the status was last cleared";
+    else if (host & FLR_STATUS_STAGING)
+        g_last_error = "a staging copy of the batched kernel completed late: the outputs of its "
+                       "work item are NaN";
     return FLR_OK;
 }
 

@@ -45,9 +45,7 @@ namespace flr {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kWindowMargin = 4;          // samples added on each side of the window estimate
-constexpr long kMaxWaitPolls = 1L << 20;  // bound on mbarrier polls for one bulk copy
-constexpr unsigned kStatusStaging = 0x10u;
+constexpr int kWindowMargin = 4;  // samples added on each side of the window estimate
 
 __device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000ll); }
 
@@ -96,9 +94,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait for the bulk copy of the current phase; true when it completed.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
-    for (long it = 0; it < kMaxWaitPolls; ++it)
+// Bounded wait for the bulk copy of the current phase (at most `polls`
+// try_wait polls); true when it completed.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, long polls) {
+    for (long it = 0; it < polls; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -806,11 +805,28 @@ __global__ void __launch_bounds__(kThreads, (kGrouped && !kDiag) ? 3 : 0)
                 mbar_expect_tx(bar, (uint32_t)W * 16u);
                 bulk_copy_g2s(hraw, src.h + wlo, (uint32_t)W * 16u, bar);
             }
-            const bool done = mbar_wait_bounded(bar, phase);
+            const bool done = mbar_wait_bounded(bar, phase, a.wait_polls);
             if (__syncthreads_or(!done)) {
+                // the copy missed the first bound: wait again with the full bound,
+                // so that it lands before this block reuses its shared memory
+                const bool landed = mbar_wait_bounded(bar, phase, kFusedWaitPolls);
+                if (__syncthreads_or(!landed)) {
+                    // still in flight: the block cannot reuse its shared memory and
+                    // leaves; its remaining items are never computed, so every
+                    // output of the launch is to be discarded
+                    if (tid == 0) raise_status(a.orb.status, kStatusStaging | kStatusStagingLost);
+                    return;
+                }
+                phase ^= 1u;
+                // the copy landed late: this item's outputs become NaN (it is not
+                // computed) and the block goes on with its next item
                 if (tid == 0) raise_status(a.orb.status, kStatusStaging);
-                mbar_wait_bounded(bar, phase);  // let a late copy land before exiting
-                return;
+                if (!kInner || src.out)
+                    for (int c = 0; c < 3; ++c)
+                        for (long i = o0 + tid; i < o1; i += kThreads) src.out[c * n + i] = qnan();
+                if (kInner && tid < 6) a.partial[wi * 6 + tid] = qnan();
+                __syncthreads();
+                continue;
             }
             phase ^= 1u;
         }

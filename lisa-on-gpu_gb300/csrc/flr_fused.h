@@ -12,6 +12,14 @@ constexpr int kFusedMaxCombos = 320;
 constexpr int kFusedMaxDepth = 16;  // links per TDI delay list
 constexpr int kFusedMaxH = 40;   // h = (order + 1) / 2 supported by the fused kernel
 constexpr int kFusedMaxGroups = kFusedMaxDepth + 1;  // distinct delay-list lengths
+// Bound on the mbarrier polls of one staging copy (the default of
+// FusedArgs::wait_polls and the bound of the second wait, see the kernel).
+constexpr long kFusedWaitPolls = 1L << 20;
+// Status bits of the fused kernel (beside those of flr_device.cuh):
+constexpr unsigned kStatusStaging = 0x10u;      // an item's copy missed its first wait:
+                                                // that item's outputs are NaN
+constexpr unsigned kStatusStagingLost = 0x20u;  // a copy never completed: a block left
+                                                // the launch, whose outputs are all invalid
 
 // One source of a batch (device copy of flr_batch_source plus derived values).
 struct FusedSource {
@@ -102,6 +110,7 @@ struct FusedArgs {
     int y_halo;                // link-stream samples computed before a tile
     int y_halo_hi;             // and after it: TDI delays only look back, so the taps
                                // of a tile's last sample reach h samples past it
+    long wait_polls;           // bound of an item's first wait for its staging copy
     int win_max;               // capacity of the staged input window [samples]
     int y_max;                 // capacity of one staged link row [samples]
     double fs;                 // sampling frequency

@@ -22,6 +22,8 @@ STATUS_BITS = {
     0x2: "A-table index out of range",
     0x4: "unknown link number",
     0x8: "TDI channel out of range",
+    0x10: "a staging copy completed late (its work item's outputs are NaN)",
+    0x20: "a staging copy never completed (discard every output of the batch)",
 }
 
 

@@ -112,6 +112,8 @@ def _plan_fns():
     lib.flr_batch_graph_launch.restype = i
     lib.flr_batch_graph_destroy.argtypes = [p]
     lib.flr_batch_graph_destroy.restype = i
+    lib.flr_batch_plan_set_wait_limit.argtypes = [p, ctypes.c_longlong]
+    lib.flr_batch_plan_set_wait_limit.restype = i
     return lib
 
 
@@ -568,9 +570,17 @@ class BatchedResponseTDI:
         return BatchGraph(self, max_sources, waveforms, diagnostics)
 
     def status(self, reset: bool = False) -> int:
-        """Kernel status bits (see include/flr_gb300.h; 0x10 = a staging copy
-        did not complete); synchronises."""
+        """Kernel status bits (see include/flr_gb300.h; 0x10 = a work item's
+        staging copy completed late and its outputs are NaN, 0x20 = a copy
+        never completed and the batch's outputs are to be discarded);
+        synchronises."""
         return self.cpp_orbits.status(reset=reset)
+
+    def _set_wait_limit(self, polls: int) -> None:
+        """Test hook: bound of each work item's first wait for its staging
+        copy in later runs (< 0: the default); see
+        flr_batch_plan_set_wait_limit."""
+        _lib.check(_plan_fns().flr_batch_plan_set_wait_limit(self._plan, int(polls)))
 
 
 class BatchGraph:
