@@ -2,36 +2,43 @@
 """Benchmark of the LISA time-domain response + TDI on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload NAME] [--no-cpu-baseline] [--batch-sources S]
-                    [--precision-sources P] [--serve-requests R]
+                    [--batch-sources S] [--no-cpu-baseline] [--precision-sources P]
+                    [--serve-requests R] [--details FILE]
 
-One step = one pass of the hot path over one source: the six link projections
-and the TDI channels.  The default workload is one galactic binary observed
-for 1 yr at dt = 5 s (6,311,629 samples) with flexing Keplerian orbits,
-2nd-generation TDI XYZ and Lagrange order 25.  The headline runs it through
-the mixed-precision fused kernel (BatchedResponseTDI, autotuned tile, 8
-tile-aligned launches over two streams per step; FP64 delays and bit-exact
-indices, double-float taps); the plain FP64 drop-in path
-(pyResponseTDI, bit-identical to the reference's CPU arithmetic) is timed on
-the same source beside it.
-
-Printed on rank 0, one JSON line:
-  value       output samples/s with the input resident in HBM (CUDA events
-              around each step, L2 flushed before each, max over ranks);
-  e2e         the same metric through BatchedResponseTDI.run_host with the
-              input in pinned host memory and X/Y/Z copied back to pinned host
-              memory, the copies overlapped with the launches;
-  roofline    the fused kernel's FP64 index-path operations per second
-              against the FP64 FMA peak measured at start-up (and its HBM
-              fraction against MEASURED_PEAKS.json); plain_fp64.roofline the
-              same for the plain path's dominant kernel;
-  cpu_baseline  the C oracle on one host core, on a bounded slice;
-  batched / precision / serving  the batching, precision and serving
-              configurations (see their sections).
-With --impl reference the CPU implementation is timed instead (all host
-cores, one independent source per process) and printed with "impl":
-"reference".  Under torchrun every rank runs its own source and its share of
-the batch (weak scaling); the reference arm runs on rank 0 only.
+Headline workload (one step = one pass of the hot path over it): the batching
+configuration -- 2048 galactic binaries with lengths log-uniform in
+2^15..2^22 samples at dt = 10 s (1.76e9 samples), f log-uniform 1e-4..1e-2 Hz,
+fdot 1e-18..1e-13, A 1e-23..1e-21, isotropic angles (seed 3), equal-arm
+orbits, 2nd-generation TDI XYZ, Lagrange order 25.  Our arm evaluates it in
+mixed precision (FP64 delays and bit-exact integer indices, double-float
+taps), all sources in one persistent launch replayed from a CUDA graph per
+step.  Printed on rank 0, one JSON line:
+  value         output samples/s with the inputs resident in HBM (28 GB, larger
+                than L2; L2 also flushed before each step), CUDA events around
+                each step, max over ranks;
+  e2e           the same through BatchedResponseTDI.run_host: waveforms in
+                page-locked host memory, channels returned to page-locked host
+                memory, copies inside the timed region;
+  roofline      the fused kernel's FP64 index-path operations per second against
+                the FP64 FMA rate measured at start-up, its HBM bytes against
+                MEASURED_PEAKS.json;
+  cpu_baseline  the C restatement of the reference's CPU path on one host core,
+                on slices of the same source list;
+  plain_fp64    the plain FP64 drop-in path (pyResponseTDI, bit-identical to the
+                reference's CPU arithmetic) on a length-matched subset of the
+                same sources, and speedup_vs_plain_fp64 = value / its rate;
+  fp64_fused    the fused kernel in its FP64 flavour on that subset;
+  accuracy      mixed vs plain FP64 on that subset (relative L2 per channel);
+  single_source the 1 yr / dt = 5 s source with flexing Keplerian orbits
+                (mixed, single launch, plain FP64, the drop-in ResponseWrapper
+                end to end with NumPy in and out);
+  precision / serving  compact summaries of those configurations (--details
+                writes the serving section's full statistics to FILE).
+With --impl reference the reference's CPU path (the C restatement) is timed
+on all host cores over slices of the same source list, printed with "impl":
+"reference" and the same "config".  Under torchrun every rank takes a share of
+the sources balanced by samples (weak scaling); the reference arm runs on rank
+0 only.
 """
 
 from __future__ import annotations
@@ -57,94 +64,129 @@ YRSID_SI = 31558149.763545603
 T_BUFFER = 1e4
 METRIC = "response+TDI output samples/s"
 UNIT = "samples/s"
-SOURCE = dict(A=1e-22, f=2e-3, fdot=1e-14)
 
-WORKLOADS = {
-    "1yr_dt5_gen2": dict(
-        desc="one galactic binary, 1 yr at dt = 5 s (6,311,629 samples), flexing Keplerian "
-             "orbits (arms +-1 %), 2nd-generation TDI XYZ, Lagrange order 25, float64",
-        dt=5.0, n=int(YRSID_SI / 5.0), orbits="kepler", tdi="2nd generation", order=25),
-    "2p21_dt5_gen2": dict(
-        desc="one galactic binary, 2^21 samples at dt = 5 s, flexing Keplerian orbits, "
-             "2nd-generation TDI XYZ, Lagrange order 25, float64 (profiling size)",
-        dt=5.0, n=2**21, orbits="kepler", tdi="2nd generation", order=25),
-    "2p18_dt10_gen1": dict(
-        desc="one galactic binary, 2^18 samples at dt = 10 s, rigid equal-arm orbits, "
-             "1st-generation TDI XYZ, Lagrange order 25, float64",
-        dt=10.0, n=2**18, orbits="equal", tdi="1st generation", order=25),
-}
-DEFAULT_WORKLOAD = "1yr_dt5_gen2"
-CPU_SLICE = 2**20  # samples per source in the CPU measurements (~3 s per pass on one core)
-HEADLINE_CHUNKS = 8  # launches per headline step (two streams: last waves overlap)
-E2E_CHUNKS = 8       # pieces of the end-to-end step's source (copy/compute overlap)
-SERVE_BATCH_SAMPLES = 2**23  # samples per serving batch at most (the server's default)
+BATCH = dict(sources=2048, seed=3, dt=10.0, log2_min=15, log2_max=22, order=25,
+             tdi="2nd generation")
+SINGLE = dict(desc="one galactic binary (A 1e-22, f 2e-3 Hz, fdot 1e-14), 1 yr at dt = 5 s "
+                   "(6,311,629 samples), flexing Keplerian orbits (arms +-1 %), 2nd-generation "
+                   "TDI XYZ, Lagrange order 25",
+              dt=5.0, n=int(YRSID_SI / 5.0), order=25, tdi="2nd generation",
+              A=1e-22, f=2e-3, fdot=1e-14)
+CPU_SLICE = 2**17         # output samples per CPU task (a slice of one source)
+SUBSET_STRIDE = 16        # plain FP64 leg: every 16th source by length (128 of 2048)
+E2E_GROUP_SAMPLES = 2**27  # samples per launch of the host pipeline
+SINGLE_CHUNKS = 8          # launches per 1 yr step (two streams: last waves overlap)
+SERVE_BATCH_SAMPLES = 2**23
 
 
-# ----------------------------------------------------------------------------- setup
+def batch_config(sources: int) -> dict:
+    """The `config` of both arms' JSON lines (identical, so the two measure
+    the same workload)."""
+    return {"workload": f"batching configuration: {sources} galactic binaries, lengths "
+                        "log-uniform 2^15..2^22 samples at dt = 10 s, f log-U 1e-4..1e-2 Hz, "
+                        "fdot log-U 1e-18..1e-13, A log-U 1e-23..1e-21, isotropic angles "
+                        f"(seed {BATCH['seed']}), equal-arm orbits, 2nd-generation TDI XYZ, "
+                        "Lagrange order 25",
+            "sources": sources, "order": BATCH["order"], "tdi": BATCH["tdi"],
+            "dt": BATCH["dt"], "t_buffer_s": T_BUFFER,
+            "l2": "inputs (16 B/sample, 28 GB) far larger than the 129 MB L2; L2 also "
+                  "flushed before each timed step"}
 
-def make_source(w: dict, n: int, seed: int):
-    from fastlisaresponse_gb300 import orbits as om
+
+def batch_sources(count: int, seed: int = BATCH["seed"]):
+    """Lengths and galactic-binary parameters of the batching configuration."""
     from fastlisaresponse_gb300 import waveforms as wf
 
-    t_max = (math.floor(n * w["dt"] / 1e4) + 3) * 1e4
-    orb = om.KeplerianOrbits(t_max=t_max) if w["orbits"] == "kepler" else \
-        om.EqualArmlengthOrbits(t_max=t_max)
     rng = np.random.default_rng(seed)
-    iota, phi0, psi = math.acos(rng.uniform(-1, 1)), rng.uniform(0, 2 * math.pi), \
-        rng.uniform(0, math.pi)
-    lam, beta = rng.uniform(0, 2 * math.pi), math.asin(rng.uniform(-1, 1))
-    h = wf.gb_waveform(SOURCE["A"], SOURCE["f"], SOURCE["fdot"], iota, phi0, psi,
-                       np.arange(n) * w["dt"])
-    return orb, np.ascontiguousarray(h), lam, beta
+    lengths = np.exp(rng.uniform(np.log(2**BATCH["log2_min"]), np.log(2**BATCH["log2_max"]),
+                                 count)).astype(np.int64)
+    return lengths, wf.draw_gb_parameters(rng, count)
 
 
-def output_samples(n: int, dt: float) -> int:
-    return n - 2 * int(T_BUFFER / dt)
+def output_samples(n, dt=BATCH["dt"]) -> int:
+    return int(n) - 2 * int(T_BUFFER / dt)
 
 
-# ------------------------------------------------------------------------ CPU side
+def orbit_t_max(n_max: int, dt: float) -> float:
+    return (math.floor(n_max * dt / 1e4) + 3) * 1e4
 
-_worker_state = {}
+
+# ----------------------------------------------------------------------------- CPU side
+
+_worker = {}
 
 
-def _cpu_worker_init(wname, n, variant):
+def _cpu_init(count, variant):
     import oracle
+    from fastlisaresponse_gb300 import orbits as om
 
-    w = WORKLOADS[wname]
-    orb, h, lam, beta = make_source(w, n, seed=12345)
-    o = oracle.OracleResponseTDI(1.0 / w["dt"], n, orb.pycppdetector_args, orb.x_base,
-                                 order=w["order"], tdi=w["tdi"], variant=variant)
-    _worker_state.update(o=o, h=h, lam=lam, beta=beta)
+    lengths, p = batch_sources(count)
+    dt = BATCH["dt"]
+    orb = om.EqualArmlengthOrbits(t_max=orbit_t_max(int(lengths.max()), dt))
+    ts = int(T_BUFFER / dt)
+    o = oracle.OracleResponseTDI(1.0 / dt, CPU_SLICE + 2 * ts, orb.pycppdetector_args,
+                                 orb.x_base, order=BATCH["order"], tdi=BATCH["tdi"],
+                                 variant=variant)
+    _worker.update(o=o, lengths=lengths, p=p)
 
 
-def _cpu_worker_run(_):
-    s = _worker_state
+def _cpu_task(task):
+    """Output samples [a, a + CPU_SLICE) of source i (the whole source if it is
+    shorter), computed as the reference's CPU path does: the slice's input
+    with its edge zones, get_projections then get_tdi_delays."""
+    from fastlisaresponse_gb300 import waveforms as wf
+
+    i, a = task
+    s = _worker
+    p, dt = s["p"], BATCH["dt"]
+    ts = int(T_BUFFER / dt)
+    n = int(s["lengths"][i])
+    n_slice = min(n, CPU_SLICE + 2 * ts)
+    start = min(a, n - n_slice)
+    t = (start + np.arange(n_slice)) * dt
+    h = wf.gb_waveform(p["A"][i], p["f"][i], p["fdot"][i], p["iota"][i], p["phi0"][i],
+                       p["psi"][i], t)
     t0 = time.perf_counter()
-    s["o"].get_projections(s["h"], s["lam"], s["beta"], t0=0.0, t_buffer=T_BUFFER)
+    s["o"].get_projections(h, p["lam"][i], p["beta"][i], t0=float(t[0]), t_buffer=T_BUFFER)
     s["o"].get_tdi_delays()
-    return time.perf_counter() - t0
+    return n_slice - 2 * ts, time.perf_counter() - t0
 
 
-def cpu_rate(wname: str, cores: int, steps: int, warmup: int, variant: str = "o3"):
-    """Samples/s of the CPU oracle over CPU_SLICE-sample sources of the workload's
-    configuration, `cores` processes each computing its own source per step."""
-    w = WORKLOADS[wname]
-    n = CPU_SLICE
-    per = output_samples(n, w["dt"])
+def _cpu_schedule(count: int, tasks: int, offset: int):
+    """`tasks` slices spread over the source list: source (offset + k) * 797
+    mod count (797 is prime to the count: every source in turn), at a start
+    that walks through the source."""
+    lengths, _ = batch_sources(count)
+    out = []
+    for k in range(offset, offset + tasks):
+        i = (k * 797) % count
+        n = int(lengths[i])
+        out.append((i, ((k * 104729) % max(1, n - CPU_SLICE)) if n > CPU_SLICE else 0))
+    return out
+
+
+def cpu_rate(count: int, cores: int, steps: int, warmup: int, tasks_per_core: int,
+             variant: str = "o3"):
+    """Output samples/s of the CPU path over slices of the batch's sources,
+    `cores` processes, `cores * tasks_per_core` slices per step."""
     ctx = mp.get_context("spawn")
-    walls = []
-    with ctx.Pool(cores, initializer=_cpu_worker_init, initargs=(wname, n, variant)) as pool:
-        for i in range(warmup + steps):
+    walls, samples = [], 0
+    per_step = cores * tasks_per_core
+    with ctx.Pool(cores, initializer=_cpu_init, initargs=(count, variant)) as pool:
+        for st in range(warmup + steps):
+            tasks = _cpu_schedule(count, per_step, st * per_step)
             t0 = time.perf_counter()
-            pool.map(_cpu_worker_run, range(cores), chunksize=1)
-            if i >= warmup:
-                walls.append(time.perf_counter() - t0)
+            res = pool.map(_cpu_task, tasks, chunksize=1)
+            wall = time.perf_counter() - t0
+            if st >= warmup:
+                walls.append(wall)
+                samples += sum(r[0] for r in res)
     total = sum(walls)
-    return dict(value=per * cores * len(walls) / total, seconds=total,
-                ms_per_step=1e3 * total / len(walls), samples_per_step=per * cores)
+    return dict(value=samples / total, seconds=total, ms_per_step=1e3 * total / len(walls),
+                samples_per_step=samples / len(walls), steps=len(walls))
 
 
-# ------------------------------------------------------------------------ GPU side
+# ----------------------------------------------------------------------------- GPU side
 
 class ClockSampler:
     """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
@@ -217,7 +259,6 @@ def measure_fp64_peak(device) -> dict:
     lib.flr_probe_pipe_rate.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_void_p, ctypes.POINTER(ctypes.c_float),
                                         ctypes.c_void_p]
-
     sms = torch.cuda.get_device_properties(device).multi_processor_count
     blocks, threads = sms * 8, 256
     sink = torch.zeros(blocks, dtype=torch.float64, device=device)
@@ -247,18 +288,18 @@ def gpu_uuid(device) -> str:
         s = str(uuid)
         return s if s.startswith("GPU-") else "GPU-" + s
     vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
-    first = vis.split(",")[device.index] if vis else str(device.index)
-    return first
+    return vis.split(",")[device.index] if vis else str(device.index)
 
 
-def load_traffic(kernel: str, workload: str):
+def load_traffic(kernel: str):
+    """DRAM bytes per computed output sample of a kernel from an ncu capture
+    (profiles/ncu_traffic.json), or None."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if not os.path.exists(path):
         return None
     with open(path) as fh:
-        table = json.load(fh)
-    entry = table.get(f"{kernel}@{workload}")
-    return None if entry is None else entry.get("bytes_per_launch")
+        entry = json.load(fh).get(kernel)
+    return entry if isinstance(entry, dict) and "bytes_per_output_sample" in entry else None
 
 
 def _events():
@@ -285,7 +326,7 @@ def _timed(fn, steps, warmup, device, kernel_events=None):
 
     Before each timed step the L2 is flushed and the stream is held for ~1 ms
     (torch.cuda._sleep) while the host queues the step, so the events bracket
-    device work only; the step times are summed."""
+    device work; the step times are summed."""
     import torch
 
     for _ in range(warmup):
@@ -319,141 +360,357 @@ def _rel_l2_rows(got, want):
     return worst
 
 
-def _config3_sources(count, seed, dt, device, rank=0, world=1):
-    """Sources drawn like the batching configuration: lengths log-uniform in
-    2^15..2^22 samples, f log-U 1e-4..1e-2 Hz, fdot log-U 1e-18..1e-13,
-    A log-U 1e-23..1e-21, isotropic angles; waveforms generated on the device
-    for this rank's shard only (sources balanced over ranks by samples)."""
+def _device_waveforms(lengths, p, idx, dt, device):
     import torch
 
     from fastlisaresponse_gb300 import waveforms as wf
-    from fastlisaresponse_gb300.dist import shard_by_samples
 
-    rng = np.random.default_rng(seed)
-    lengths = np.exp(rng.uniform(np.log(2**15), np.log(2**22), count)).astype(np.int64)
-    p = wf.draw_gb_parameters(rng, count)
-    mine = shard_by_samples(lengths, rank, world)
     hs = []
-    for i in mine:
+    for i in idx:
         t = torch.arange(int(lengths[i]), dtype=torch.float64, device=device) * dt
         hs.append(wf.gb_waveform(p["A"][i], p["f"][i], p["fdot"][i], p["iota"][i],
                                  p["phi0"][i], p["psi"][i], t))
-    return lengths, mine, hs, p["lam"][mine], p["beta"][mine]
+    return hs
 
 
-def run_batch_section(args, device, peaks, rank=0, world=1):
-    """The batching configuration: all sources (2048 by default) in one
-    persistent launch of the mixed kernel, replayed from the CUDA graph of its
-    size bucket, against the FP64 fused kernel on the first 256 sources (whose
-    rate does not depend on the batch size; timing all 2048 in FP64 would take
-    about a minute).  Under torchrun the sources are sharded over the ranks
-    (no collective on the data path; the job time is the slowest rank's)."""
+def _timed_wrapped(lib_obj, names, holder):
+    """Wrap the named methods of lib_obj so that, while holder["on"], CUDA
+    events bracket each call on the current stream (holder[name] collects
+    them); returns a function that restores the originals."""
+    saved = {n: getattr(lib_obj, n) for n in names}
+
+    def make(name, fn):
+        def inner(*a, **k):
+            if not holder["on"]:
+                return fn(*a, **k)
+            e0, e1 = _events()
+            e0.record()
+            rc = fn(*a, **k)
+            e1.record()
+            holder[name].append((e0, e1))
+            return rc
+        return inner
+
+    for n, fn in saved.items():
+        holder.setdefault(n, [])
+        setattr(lib_obj, n, make(n, fn))
+
+    def restore():
+        for n, fn in saved.items():
+            setattr(lib_obj, n, fn)
+    return restore
+
+
+def _mean_ms(pairs):
+    return statistics.mean(a.elapsed_time(b) for a, b in pairs)
+
+
+def _unit_lists(tb):
+    lists = []
+    for u in range(tb["num_units"]):
+        st, ln = tb["unit_starts"][u], tb["unit_lengths"][u]
+        lists.append([x for x in tb["tdi_link_combinations"][st:st + ln] if x != -11])
+    return lists
+
+
+def run_headline(args, device, peaks, rank, world):
+    """The batching configuration in mixed precision (value, e2e, roofline),
+    with the plain FP64 drop-in path, the FP64 fused kernel and the mixed
+    kernel on a length-matched subset beside it."""
     import torch
 
     import fastlisaresponse_gb300 as flr
-    from fastlisaresponse_gb300.dist import max_over_ranks
+    from fastlisaresponse_gb300 import _lib, perfmodel
+    from fastlisaresponse_gb300.dist import max_over_ranks, shard_by_samples
 
-    dt = 10.0
-    lengths, mine, hs, lam, beta = _config3_sources(args.batch_sources, seed=3, dt=dt,
-                                                    device=device, rank=rank, world=world)
-    orb = flr.EqualArmlengthOrbits(t_max=(math.floor(lengths.max() * dt / 1e4) + 3) * 1e4)
-    ts = int(T_BUFFER / dt)
-    n_out = int(sum(int(n) - 2 * ts for n in lengths))
-    sub = list(range(min(256, len(mine))))
-    n_sub = int(sum(int(lengths[mine[i]]) - 2 * ts for i in sub))
-    res = {"sources": int(args.batch_sources), "samples": int(lengths.sum()),
-           "output_samples": n_out, "sources_per_rank": len(mine),
-           "workload": "batching configuration: lengths log-uniform 2^15..2^22 at dt = 10 s, "
-                       "f log-U 1e-4..1e-2 Hz, fdot log-U 1e-18..1e-13, A log-U 1e-23..1e-21, "
-                       "equal-arm orbits, 2nd-gen TDI XYZ, order 25",
-           "hbm_bytes_inputs_outputs": int(lengths.sum()) * 40}
+    dt = BATCH["dt"]
+    lengths, p = batch_sources(args.batch_sources)
+    mine = list(shard_by_samples(lengths, rank, world))
+    orb = flr.EqualArmlengthOrbits(t_max=orbit_t_max(int(lengths.max()), dt))
+    hs = _device_waveforms(lengths, p, mine, dt, device)
+    lam, beta = p["lam"][mine], p["beta"][mine]
+    n_out = sum(output_samples(lengths[i]) for i in mine)
+    res = {}
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # --- value: every source of this rank in one launch, through its graph bucket
     tune = [int(lengths[i]) for i in mine[:32]]
-    # mixed: every source of this rank in one launch, through its graph bucket
-    bat = flr.BatchedResponseTDI(1 / dt, order=25, tdi="2nd generation", orbits=orb,
-                                 precision="mixed", tile="auto", tune_lengths=tune)
-    out_m = [torch.empty((3, int(lengths[i])), dtype=torch.float64, device=device) for i in mine]
-    steps = max(1, min(args.steps, 3))
-    secs = max_over_ranks([_timed(lambda: bat(hs, lam, beta, out=out_m, use_graph=True),
-                                  steps, 1, device)], device=device)[0]
-    assert bat.status() == 0, flr.describe_status(bat.status())
-    res["mixed"] = {"value": n_out * steps / secs, "ms_per_step": 1e3 * secs / steps,
-                    "steps": steps, "plan": bat.plan_info, "tune": bat.tune,
-                    "path": "BatchedResponseTDI(precision='mixed', use_graph=True): one graph "
-                            "replay (staging copy + fused kernel) per step"}
-    del bat
-    # fp64 on the first sources
-    bat = flr.BatchedResponseTDI(1 / dt, order=25, tdi="2nd generation", orbits=orb,
-                                 precision="fp64", tile="auto", tune_lengths=tune)
-    holder = {}
+    bat = flr.BatchedResponseTDI(1 / dt, order=BATCH["order"], tdi=BATCH["tdi"], orbits=orb,
+                                 precision="mixed", tile="auto", tune_lengths=tune,
+                                 force_backend=device)
+    outs = [torch.empty((3, int(lengths[i])), dtype=torch.float64, device=device) for i in mine]
 
     def step():
-        holder["o"] = bat([hs[i] for i in sub], lam[sub], beta[sub])
+        bat(hs, lam, beta, out=outs, use_graph=True)
 
-    secs = max_over_ranks([_timed(step, 1, 1, device)], device=device)[0]
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(device)
+    clocks = ClockSampler(gpu_uuid(device))
+    clocks.start()
+    time.sleep(0.4)
+    barrier()
+    secs = _timed(step, args.steps, 0, device)
+    barrier()
+    res["clocks"] = clocks.stop()
     assert bat.status() == 0, flr.describe_status(bat.status())
-    res["fp64"] = {"value": n_sub / secs, "ms_per_step": 1e3 * secs, "steps": 1,
-                   "sources": len(sub), "plan": bat.plan_info, "tune": bat.tune}
-    del bat
-    res["speedup_mixed_over_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
-    res["max_rel_l2_mixed_vs_fp64"] = max_over_ranks(
-        [max(_rel_l2_rows(out_m[i], holder["o"][k]) for k, i in enumerate(sub))],
-        device=device)[0]
-    res["accuracy_sources"] = len(sub)
-    del holder
-    # the sampler's form: <h|d> and <h|h> per source formed in the kernel, the
-    # channels never stored (data = the mixed outputs themselves)
-    bat = flr.BatchedResponseTDI(1 / dt, order=25, tdi="2nd generation", orbits=orb,
-                                 precision="mixed", tile="auto", tune_lengths=tune)
+    launch_secs = secs / args.steps  # one graph replay = staging copy + one fused launch
+    job_secs = max_over_ranks([secs], device=device)[0]
+    res["value"] = n_out * world * args.steps / job_secs
+    res["ms_per_step"] = 1e3 * job_secs / args.steps
+    res["plan"] = {k: bat.plan_info[k] for k in ("tile", "grid", "smem_bytes", "grouped")}
+
+    # --- roofline of the fused kernel (one launch per step)
+    tb = bat.tdi_sets[0]
+    lists = _unit_lists(tb)
+    idx_ops = perfmodel.mixed_index_ops_grouped(num_groups=len({len(x) for x in lists}),
+                                                max_len=max(len(x) for x in lists))
+    measured = {}
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as fh:
+            measured = json.load(fh)
+    hbm_peak = measured.get("hbm_gbs")
+    fused_bytes = 40 * n_out  # complex input in, three channels out
+    traffic = load_traffic("fused_kernel_mixed_grouped")
+    res["roofline"] = {
+        "bound": "fp64",
+        "kernel": "fused_kernel<mixed, grouped> (flr_fused.cu), equal arms",
+        "achieved": idx_ops["total"] * n_out / launch_secs / 1e9,
+        "peak": peaks["fp64_fma"] / 1e9,
+        "unit": "G FP64-ops/s",
+        "frac": idx_ops["total"] * n_out / launch_secs / peaks["fp64_fma"],
+        "definition": "FP64 operations of the bit-exact delay/index path per output sample "
+                      f"(perfmodel.mixed_index_ops_grouped: {idx_ops['total']}) x output "
+                      "samples / one launch's CUDA-event time; the double-float taps run on "
+                      "the FP32 pipe, not counted; peak = FP64 FMA probe of this run "
+                      "(MEASURED_PEAKS.json has no FP64 figure)",
+        "launch_ms": 1e3 * launch_secs,
+        "traffic": (traffic["bytes_per_output_sample"] * n_out) if traffic else None,
+        "traffic_source": traffic["source"] if traffic else None,
+        "hbm": {"algorithmic_bytes": fused_bytes,
+                "achieved_gbs": fused_bytes / launch_secs / 1e9, "peak_gbs": hbm_peak,
+                "frac": (fused_bytes / launch_secs / 1e9 / hbm_peak) if hbm_peak else None},
+    }
+
+    # --- e2e: host memory in and out through run_host (grouped launches)
+    # (two page-locked regions, one view per source: the inputs and the channels)
+    barrier()
+    n_in = sum(int(lengths[i]) for i in mine)
+    h_all = flr.HostArray(n_in, np.complex128)
+    o_all = flr.HostArray(3 * n_in)
+    h_host, o_host, off = [], [], 0
+    for i, h in zip(mine, hs):
+        n = int(lengths[i])
+        h_host.append(h_all.tensor[off:off + n])
+        o_host.append(o_all.tensor[3 * off:3 * (off + n)].view(3, n))
+        h_host[-1].copy_(h)
+        off += n
+    bat_h = flr.BatchedResponseTDI(1 / dt, order=BATCH["order"], tdi=BATCH["tdi"], orbits=orb,
+                                   precision="mixed", tile=bat.plan_info["tile"],
+                                   force_backend=device)
+
+    def e2e_step():
+        bat_h.run_host(h_host, lam, beta, out=o_host, group_samples=E2E_GROUP_SAMPLES)
+
+    e2e_secs = max_over_ranks([_timed(e2e_step, args.steps, args.warmup, device)],
+                              device=device)[0]
+    torch.cuda.synchronize(device)
+    assert bat_h.status() == 0
+    e2e_same = all(torch.equal(o, d.cpu()) for o, d in zip(o_host[:16], outs[:16]))
+    del h_host, o_host, bat_h
+    h_all.release()
+    o_all.release()
+    del h_all, o_all
+    res["e2e"] = {"value": n_out * world * args.steps / e2e_secs, "unit": UNIT,
+                  "h2d_bytes_per_step": 16 * n_in, "d2h_bytes_per_step": 24 * n_in,
+                  "api": "BatchedResponseTDI.run_host: waveforms in page-locked host memory "
+                         "(HostArray), channels back to page-locked host memory, "
+                         f"~2^{int(math.log2(E2E_GROUP_SAMPLES))} samples per launch, copies "
+                         "overlapped with the launches",
+                  "same_bits_as_device_run": bool(e2e_same)}
+
+    # --- the plain FP64 drop-in path, the FP64 fused kernel and the mixed kernel on a
+    # length-matched subset: every SUBSET_STRIDE-th source in length order
+    order = sorted(range(len(mine)), key=lambda k: int(lengths[mine[k]]))
+    sub = order[SUBSET_STRIDE // 2::SUBSET_STRIDE]
+    sub_out = sum(output_samples(lengths[mine[k]]) for k in sub)
+    sub_len = [int(lengths[mine[k]]) for k in sub]
+    resp = {}
+    for k in sub:  # one drop-in instance per source length (the API's num_pts)
+        resp[k] = flr.pyResponseTDI(1 / dt, int(lengths[mine[k]]), order=BATCH["order"],
+                                    tdi=BATCH["tdi"], orbits=orb, force_backend=device)
+    pev = {"on": False}
+    lib = _lib.lib()
+    restore = _timed_wrapped(lib, ["flr_get_response", "flr_get_tdi_delays"], pev)
+
+    def plain_step():
+        for k in sub:
+            resp[k].get_projections(hs[k], float(lam[k]), float(beta[k]), t0=0.0,
+                                    t_buffer=T_BUFFER)
+            resp[k].get_tdi_delays()
+
+    plain_steps = max(1, min(args.steps, 2))
+    plain_secs = _timed(plain_step, plain_steps, 1, device, kernel_events=pev)
+    restore()
+    assert all(r.status() == 0 for r in resp.values())
+    plain_rate = sub_out * plain_steps / plain_secs
+    kern = {"response": _mean_ms(pev["flr_get_response"]),
+            "tdi": _mean_ms(pev["flr_get_tdi_delays"])}
+    # mixed on the subset (same sources), and its accuracy against the plain path
+    sub_outs = [outs[k] for k in sub]
+    acc = max(_rel_l2_rows(o, resp[k].XYZ) for o, k in zip(sub_outs, sub))
+    mixed_sub_secs = _timed(lambda: bat([hs[k] for k in sub], lam[sub], beta[sub],
+                                        out=sub_outs), 2, 1, device)
+    # FP64 fused on the subset: bit-identical to the plain path
+    bat64 = flr.BatchedResponseTDI(1 / dt, order=BATCH["order"], tdi=BATCH["tdi"], orbits=orb,
+                                   precision="fp64", tile="auto", tune_lengths=sub_len[:32],
+                                   force_backend=device)
     box = {}
 
-    def inner_step():
-        box["i"] = bat.inner_products(hs, lam, beta, out_m)
+    def fp64_step():
+        box["o"] = bat64([hs[k] for k in sub], lam[sub], beta[sub])
 
-    secs = max_over_ranks([_timed(inner_step, steps, 1, device)], device=device)[0]
-    assert bat.status() == 0, flr.describe_status(bat.status())
-    hh = box["i"][:, 1, :]
-    hh_ref = torch.stack([(o[:, ts:o.shape[1] - ts] ** 2).sum(dim=1) for o in out_m])
-    res["inner_products"] = {
-        "value": n_out * steps / secs, "ms_per_step": 1e3 * secs / steps, "steps": steps,
-        "path": "BatchedResponseTDI.inner_products: per-source <h|d>, <h|h> per channel from "
-                "the fused kernel, no channel stored (24 B/sample of HBM writes saved)",
-        "max_rel_diff_hh_vs_stored": float(((hh - hh_ref).abs() / hh_ref.abs()).max().item())}
-    del bat, out_m, hs, box
+    fp64_secs = _timed(fp64_step, 1, 1, device)
+    assert bat64.status() == 0
+    fp64_same = all(torch.equal(o, resp[k].XYZ) for o, k in zip(box["o"], sub))
+    del box, bat64
+    # plain path roofline: its dominant kernel, reference-arithmetic FP64 work
+    counts = perfmodel.counts_per_sample(BATCH["order"], tb["num_units"],
+                                         sum(len(x) for x in lists))
+    div_cost = peaks["fp64_fma"] / peaks["fp64_div"]
+    dom = max(kern, key=kern.get)
+    c = counts[dom]
+    r0 = resp[sub[-1]]
+    start = {"response": r0.projections_start_ind, "tdi": r0.tdi_start_ind}[dom]
+    computed = sum(int(lengths[mine[k]]) - 2 * start for k in sub) / len(sub)
+    psecs = kern[dom] * 1e-3
+    res["plain_fp64"] = {
+        "value": plain_rate, "sources": len(sub), "output_samples": sub_out,
+        "ms_per_step": 1e3 * plain_secs / plain_steps,
+        "path": "pyResponseTDI.get_projections + get_tdi_delays per source (drop-in API, "
+                f"device inputs), every {SUBSET_STRIDE}th source of the batch in length order",
+        "roofline_frac": perfmodel.fp64_slots(c, div_cost) * computed / psecs
+        / peaks["fp64_fma"],
+        "roofline_frac_division_as_one_op": (c["ops"] + c["divs"]) * computed / psecs
+        / peaks["fp64_fma"],
+        "roofline_kernel": f"{dom}_plain_kernel (mean launch {kern[dom]:.2f} ms)"}
+    res["fp64_fused"] = {"value": sub_out / fp64_secs, "sources": len(sub),
+                         "bit_identical_to_plain": bool(fp64_same)}
+    res["mixed_on_subset"] = sub_out * 2 / mixed_sub_secs
+    res["accuracy"] = {"max_rel_l2_vs_plain_fp64": acc, "bound": 1e-6,
+                       "per": "TDI channel, the subset's sources"}
+    res["gpu_launches"] = args.steps  # one fused kernel per graph replay
+    del outs, hs, resp
     torch.cuda.empty_cache()
     return res
 
 
-def _err_stats(got, want):
-    """Per-row relative L2 and max error (max |got - want| / max |want|)."""
+def run_single_source(args, device, peaks):
+    """The 1 yr source: mixed (chunked and one launch), plain FP64, and the
+    drop-in ResponseWrapper end to end with NumPy in and out."""
     import torch
 
-    d = got - want
-    num = torch.linalg.vector_norm(d, dim=1)
-    den = torch.linalg.vector_norm(want, dim=1)
-    mx = d.abs().amax(dim=1) / want.abs().amax(dim=1).clamp_min(1e-300)
-    return (num / den.clamp_min(1e-300)).cpu().numpy(), mx.cpu().numpy()
+    import fastlisaresponse_gb300 as flr
+    from fastlisaresponse_gb300 import batch as bm
+    from fastlisaresponse_gb300 import perfmodel
+    from fastlisaresponse_gb300 import waveforms as wf
+
+    w = SINGLE
+    n, dt = w["n"], w["dt"]
+    orb = flr.KeplerianOrbits(t_max=orbit_t_max(n, dt))
+    rng = np.random.default_rng(1)
+    iota, phi0, psi = math.acos(rng.uniform(-1, 1)), rng.uniform(0, 2 * math.pi), \
+        rng.uniform(0, math.pi)
+    lam, beta = rng.uniform(0, 2 * math.pi), math.asin(rng.uniform(-1, 1))
+    h = np.ascontiguousarray(wf.gb_waveform(w["A"], w["f"], w["fdot"], iota, phi0, psi,
+                                            np.arange(n) * dt))
+    h_dev = torch.as_tensor(h, device=device)
+    n_out = output_samples(n, dt)
+    steps = max(1, min(args.steps, 5))
+    bat = flr.BatchedResponseTDI(1 / dt, order=w["order"], tdi=w["tdi"], orbits=orb,
+                                 precision="mixed", tile="auto", tune_lengths=[n],
+                                 force_backend=device)
+    out = torch.empty((3, n), dtype=torch.float64, device=device)
+    chunked = _timed(lambda: bat([h_dev], lam, beta, out=[out], chunks=SINGLE_CHUNKS), steps,
+                     2, device)
+    ev = {"on": False}
+    lib = bm._plan_fns()
+    restore = _timed_wrapped(lib, ["flr_batch_run"], ev)
+    one = _timed(lambda: bat([h_dev], lam, beta, out=[out]), steps, 1, device, kernel_events=ev)
+    restore()
+    assert bat.status() == 0
+    launch_s = _mean_ms(ev["flr_batch_run"]) * 1e-3
+    tb = bat.tdi_sets[0]
+    idx_ops = perfmodel.mixed_index_ops(
+        tb["num_units"], perfmodel.prefix_shared_subtractions(_unit_lists(tb)))
+    # plain FP64 drop-in path
+    resp = flr.pyResponseTDI(1 / dt, n, order=w["order"], tdi=w["tdi"], orbits=orb,
+                             force_backend=device)
+
+    def plain_step():
+        resp.get_projections(h_dev, lam, beta, t0=0.0, t_buffer=T_BUFFER)
+        resp.get_tdi_delays()
+
+    plain_steps = max(1, min(args.steps, 3))
+    plain = _timed(plain_step, plain_steps, 1, device)
+    acc = _rel_l2_rows(out, resp.XYZ)
+    # the drop-in wrapper end to end: NumPy waveform in, NumPy channels out
+    wrapped = {}
+    prm = [w["A"], w["f"], w["fdot"], iota, phi0, psi, lam, beta]
+    for prec, k in (("mixed", 5), (None, 3)):
+        rw = flr.ResponseWrapper(lambda *a, **kw: h, n * dt / YRSID_SI, dt, 6, 7, orbits=orb,
+                                 order=w["order"], tdi=w["tdi"], n_overide=n, precision=prec,
+                                 remove_garbage=False, force_backend=device)
+        holder = {}
+
+        def e2e_step():
+            holder["x"] = [c.cpu().numpy() for c in rw(*prm)]
+
+        k = max(1, min(args.steps, k))
+        wrapped["mixed" if prec else "plain_fp64"] = n_out * k / _timed(e2e_step, k, 1, device)
+    return {
+        "workload": w["desc"],
+        "mixed": n_out * steps / chunked,
+        "mixed_single_launch": n_out * steps / one,
+        "plain_fp64": n_out * plain_steps / plain,
+        "speedup_vs_plain_fp64": (n_out * steps / chunked) / (n_out * plain_steps / plain),
+        "fp64_index_roofline_frac": idx_ops["total"] * n_out / launch_s / peaks["fp64_fma"],
+        "launch_ms": 1e3 * launch_s,
+        "max_rel_l2_vs_plain_fp64": acc,
+        "e2e_dropin_numpy": wrapped,
+        "e2e_api": "ResponseWrapper (waveform_gen returning a NumPy array; precision='mixed' "
+                   "or the plain path) and .cpu().numpy() of the channels, per step",
+    }
 
 
 def run_precision_section(args, device):
     """Precision configuration: sources of 2^20 samples at dt = 10 s drawn as
-    in the batching configuration, Lagrange orders 25 and 45.  The mixed path
-    is compared with the FP64 fused path (bit-identical to the oracle and the
-    plain path) per link and per X/Y/Z channel, and its integer delay indices
-    (receiver, emitter, every TDI unit) with the FP64 path's, bit for bit."""
+    in the batching configuration, Lagrange orders 25 and 45; mixed against the
+    FP64 fused path (bit-identical to the oracle) per link and per channel, and
+    integer delay indices bit for bit."""
     import torch
 
     import fastlisaresponse_gb300 as flr
+
+    def err_stats(got, want):
+        d = got - want
+        num = torch.linalg.vector_norm(d, dim=1)
+        den = torch.linalg.vector_norm(want, dim=1)
+        mx = d.abs().amax(dim=1) / want.abs().amax(dim=1).clamp_min(1e-300)
+        return (num / den.clamp_min(1e-300)).cpu().numpy(), mx.cpu().numpy()
 
     dt, n = 10.0, 2**20
     count = args.precision_sources
     rng = np.random.default_rng(4)
     p = flr.waveforms.draw_gb_parameters(rng, count)
-    orb = flr.EqualArmlengthOrbits(t_max=(math.floor(n * dt / 1e4) + 3) * 1e4)
+    orb = flr.EqualArmlengthOrbits(t_max=orbit_t_max(n, dt))
     t = torch.arange(n, dtype=torch.float64, device=device) * dt
     chunk = 16
-    res = {"workload": f"{count} galactic binaries x 2^20 samples at dt = 10 s drawn as in the "
-                       "batching configuration, equal-arm orbits, 2nd-gen TDI XYZ",
-           "sources": count, "reference": "FP64 fused path (bit-identical to the oracle)"}
+    res = {"sources": count, "samples_per_source": n}
     for order in (25, 45):
         tb = 1e4 if order <= 25 else 2e4  # order 45 needs the longer garbage margin
         plans = {prec: flr.BatchedResponseTDI(1 / dt, order=order, tdi="2nd generation",
@@ -462,14 +719,14 @@ def run_precision_section(args, device):
                  for prec in ("fp64", "mixed")}
         ts = plans["fp64"].tdi_start_ind
         sl = slice(ts, n - ts)
-        link_l2, link_max, chan_l2, chan_max = [], [], [], []
-        mism = {"d_rec": 0, "d_em": 0, "d_tdi": 0}
+        link_l2, chan_l2, chan_max = [], [], []
+        mism = 0
         secs = {"fp64": 0.0, "mixed": 0.0}
         for c0 in range(0, count, chunk):
-            idx = range(c0, min(count, c0 + chunk))
+            idx = list(range(c0, min(count, c0 + chunk)))
             hs = [flr.gb_waveform(p["A"][i], p["f"][i], p["fdot"][i], p["iota"][i],
                                   p["phi0"][i], p["psi"][i], t) for i in idx]
-            lam, beta = p["lam"][list(idx)], p["beta"][list(idx)]
+            lam, beta = p["lam"][idx], p["beta"][idx]
             runs = {}
             for prec, bat in plans.items():
                 bat(hs[:1], lam[:1], beta[:1])  # warm-up
@@ -484,43 +741,32 @@ def run_precision_section(args, device):
             for j in range(len(hs)):
                 (o64, d64), (omx, dmx) = [(runs[k][0][j], runs[k][1][j])
                                           for k in ("fp64", "mixed")]
-                for key in mism:
-                    mism[key] += int((dmx[key][:, sl] != d64[key][:, sl]).sum().item())
-                a, b = _err_stats(dmx["y"][:, sl], d64["y"][:, sl])
-                link_l2.append(a)
-                link_max.append(b)
-                a, b = _err_stats(omx[:, sl], o64[:, sl])
+                for key in ("d_rec", "d_em", "d_tdi"):
+                    mism += int((dmx[key][:, sl] != d64[key][:, sl]).sum().item())
+                link_l2.append(err_stats(dmx["y"][:, sl], d64["y"][:, sl])[0])
+                a, b = err_stats(omx[:, sl], o64[:, sl])
                 chan_l2.append(a)
                 chan_max.append(b)
             del runs, hs
-        link_l2, link_max = np.asarray(link_l2), np.asarray(link_max)
-        chan_l2, chan_max = np.asarray(chan_l2), np.asarray(chan_max)
+        link_l2, chan_l2 = np.asarray(link_l2), np.asarray(chan_l2)
         n_out = count * (n - 2 * ts)
         res[f"order_{order}"] = {
-            "t_buffer_s": tb,
-            "per_link": {str(k): {"rel_l2_max": float(link_l2[:, k].max()),
-                                  "rel_l2_median": float(np.median(link_l2[:, k])),
-                                  "max_err_max": float(link_max[:, k].max())}
-                         for k in range(6)},
-            "per_channel": {ch: {"rel_l2_max": float(chan_l2[:, k].max()),
-                                 "rel_l2_median": float(np.median(chan_l2[:, k])),
-                                 "max_err_max": float(chan_max[:, k].max())}
-                            for k, ch in enumerate("XYZ")},
+            "link_rel_l2_max": float(link_l2.max()),
+            "channel_rel_l2_max": float(chan_l2.max()),
+            "channel_rel_l2_median": float(np.median(chan_l2)),
+            "channel_max_err_max": float(np.max(chan_max)),
             "index_mismatches": mism,
-            "samples_per_s": {prec: n_out / s for prec, s in secs.items()},
-            "speedup_mixed_over_fp64": secs["fp64"] / secs["mixed"],
+            "mixed_samples_per_s": n_out / secs["mixed"],
+            "fp64_samples_per_s": n_out / secs["fp64"],
         }
         del plans
         torch.cuda.empty_cache()
-    res["max_err_definition"] = "max |mixed - fp64| / max |fp64| per row"
     return res
 
 
 def run_serving_section(args, device):
     """Open-loop Poisson request streams against ResponseServer: saturation
     throughput, then p50/p99 latency at rates below it."""
-    import threading
-
     import torch
 
     import fastlisaresponse_gb300 as flr
@@ -533,15 +779,8 @@ def run_serving_section(args, device):
     params = [(p["A"][i], p["f"][i], p["fdot"][i], p["iota"][i], p["phi0"][i], p["psi"][i],
                p["lam"][i], p["beta"][i]) for i in range(count)]
     sets = rng.integers(0, 2, count)
-    orb = flr.EqualArmlengthOrbits(t_max=(math.floor(lengths.max() * dt / 1e4) + 3) * 1e4)
-    out = {"workload": "open-loop Poisson requests: lengths log-uniform 2^14..2^22 at dt = 10 s, "
-                       "1st/2nd-gen TDI 50/50, galactic-binary parameters drawn as in the "
-                       "batching configuration, waveforms generated on the device, mixed "
-                       "precision, 160 GB admission budget, 2 streams",
-           "requests_per_rate": count, "mean_samples": float(lengths.mean())}
-
-    # batched throughput of the same requests (the first 2000 at most: ~60 GB)
-    # in one launch pair (reference point)
+    orb = flr.EqualArmlengthOrbits(t_max=orbit_t_max(int(lengths.max()), dt))
+    out = {"requests_per_rate": count}
     bat = flr.BatchedResponseTDI(1 / dt, tdi=["1st generation", "2nd generation"], orbits=orb,
                                  precision="mixed", force_backend=device)
     nb = min(count, 2000)
@@ -556,10 +795,8 @@ def run_serving_section(args, device):
     e1.record()
     torch.cuda.synchronize(device)
     del outs, hs
-    secs = e0.elapsed_time(e1) * 1e-3
-    n_out = int(sum(int(n) - 2000 for n in lengths[:nb]))
-    out["batched_throughput_samples_per_s"] = n_out / secs
-    out["batched_reference_requests"] = nb
+    batched = sum(output_samples(nn) for nn in lengths[:nb]) / (e0.elapsed_time(e1) * 1e-3)
+    out["batched_samples_per_s"] = batched
     del bat
     torch.cuda.empty_cache()
 
@@ -585,282 +822,97 @@ def run_serving_section(args, device):
             th.join()
             while len(srv.completed) < count:
                 time.sleep(0.005)
-            st = srv.stats()
-        return st
+            return srv.stats()
 
     sat = run(None)
-    out["saturation"] = sat
+    out["saturation_samples_per_s"] = sat["throughput_samples_per_s"]
     cap = sat["throughput_requests_per_s"]
     out["rates"] = []
+    full = {"saturation": sat, "rates": []}
     for frac in (0.5, 0.8, 0.9):
         st = run(frac * cap)
-        st["offered_requests_per_s"] = frac * cap
-        st["fraction_of_batched_throughput"] = (st["throughput_samples_per_s"] /
-                                                out["batched_throughput_samples_per_s"])
-        out["rates"].append(st)
-    return out
+        full["rates"].append(st)
+        out["rates"].append({"of_saturation": frac, "p50_ms": st["p50_ms"],
+                             "p99_ms": st["p99_ms"],
+                             "of_batched": st["throughput_samples_per_s"] / batched})
+    return out, full
 
 
-def run_ours(args, rank, world, device):
-    import torch
-
-    import fastlisaresponse_gb300 as flr
-    from fastlisaresponse_gb300 import _lib, perfmodel
-
-    w = WORKLOADS[args.workload]
-    n, dt = w["n"], w["dt"]
-    orb, h, lam, beta = make_source(w, n, seed=1 + rank)
-    n_out = output_samples(n, dt)
-    h_dev = torch.as_tensor(h, device=device)
-    lib = _lib.lib()
+def run_ours(args, rank, world, device, cpu_line):
     peaks = measure_fp64_peak(device)
-
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-
-    # --- headline: mixed-precision fused path (BatchedResponseTDI, one source,
-    # HEADLINE_CHUNKS tile-aligned launches over two streams; same bits as one)
-    bat = flr.BatchedResponseTDI(1.0 / dt, order=w["order"], tdi=w["tdi"], orbits=orb,
-                                 precision="mixed", force_backend=device, tile="auto",
-                                 tune_lengths=[n])
-    out_dev = torch.empty((3, n), dtype=torch.float64, device=device)
-    held = {}
-
-    def mixed_step():
-        held["mixed"] = bat([h_dev], lam, beta, out=[out_dev], chunks=HEADLINE_CHUNKS)[0]
-
-    for _ in range(args.warmup):
-        mixed_step()
-    torch.cuda.synchronize(device)
-    clocks = ClockSampler(gpu_uuid(device))
-    clocks.start()
-    time.sleep(0.4)
-    barrier()
-    elapsed = _timed(mixed_step, args.steps, 0, device)
-    barrier()
-    clock_info = clocks.stop()
-    assert bat.status() == 0, flr.describe_status(bat.status())
-
-    # --- the fused kernel alone: single launches, CUDA events around each on
-    # its stream (the roofline's per-launch duration)
-    ev = {"on": False, "fused": []}
-    run_fn = lib.flr_batch_run
-
-    def timed_run(*a):
-        if not ev["on"]:
-            return run_fn(*a)
-        e0, e1 = _events()
-        e0.record()
-        rc = run_fn(*a)
-        e1.record()
-        ev["fused"].append((e0, e1))
-        return rc
-
-    lib.flr_batch_run = timed_run
-    one = {}
-
-    def single_step():
-        one["o"] = bat([h_dev], lam, beta)[0]
-
-    single_elapsed = _timed(single_step, max(1, min(args.steps, 5)), 1, device, kernel_events=ev)
-    lib.flr_batch_run = run_fn
-    assert torch.equal(one["o"], held["mixed"])  # chunked launches: the same bits
-
-    # --- the plain FP64 drop-in path on the same source
-    resp = flr.pyResponseTDI(1.0 / dt, n, order=w["order"], tdi=w["tdi"], orbits=orb,
-                             force_backend=device)
-    pev = {"on": False, "response": [], "tdi": []}
-
-    def wrap(name, fn):
-        def inner(*a, **k):
-            if not pev["on"]:
-                return fn(*a, **k)
-            e0, e1 = _events()
-            e0.record()
-            fn(*a, **k)
-            e1.record()
-            pev[name].append((e0, e1))
-        return inner
-
-    resp.cpp_response.get_response_wrap = wrap("response", resp.cpp_response.get_response_wrap)
-    resp.cpp_response.get_tdi_delays_wrap = wrap("tdi", resp.cpp_response.get_tdi_delays_wrap)
-
-    def plain_step():
-        resp.get_projections(h_dev, lam, beta, t0=0.0, t_buffer=T_BUFFER)
-        resp.get_tdi_delays()
-
-    plain_steps = max(1, min(args.steps, 5))
-    plain_elapsed = _timed(plain_step, plain_steps, 1, device, kernel_events=pev)
-    assert resp.status() == 0
-    max_rel = _rel_l2_rows(held["mixed"], resp.XYZ)
-
-    # --- end to end through BatchedResponseTDI.run_host: pinned host in, pinned
-    # host out, copies overlapped with the computation (4 chunks)
-    h_pin = torch.from_numpy(h).pin_memory()
-    out_pin = torch.empty((3, n), dtype=torch.float64).pin_memory()
-
-    def e2e_step():
-        bat.run_host([h_pin], lam, beta, out=[out_pin], chunks=E2E_CHUNKS)
-
-    barrier()
-    e2e_elapsed = _timed(e2e_step, args.steps, args.warmup, device)
-    barrier()
-
-    from fastlisaresponse_gb300.dist import max_over_ranks
-
-    elapsed, e2e_elapsed = max_over_ranks([elapsed, e2e_elapsed], device=device)
-
-    # --- rooflines
-    tables = resp.tdi_tables_host
-    lists = []
-    for u in range(tables["num_units"]):
-        st, ln = tables["unit_starts"][u], tables["unit_lengths"][u]
-        lists.append([x for x in tables["tdi_link_combinations"][st:st + ln] if x != -11])
-    n_delay_links = sum(len(x) for x in lists)
-    measured = {}
-    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(peaks_path):
-        with open(peaks_path) as fh:
-            measured = json.load(fh)
-    hbm_peak = measured.get("hbm_gbs")
-    peak = peaks["fp64_fma"]
-    div_cost = peaks["fp64_fma"] / peaks["fp64_div"]
-
-    fused_ms = 1e3 * statistics.mean(a.elapsed_time(b) * 1e-3 for a, b in ev["fused"])
-    idx_ops = perfmodel.mixed_index_ops(tables["num_units"],
-                                        perfmodel.prefix_shared_subtractions(lists))
-    fused_secs = fused_ms * 1e-3
-    fused_bytes = 40 * n_out  # complex input in, three channels out
-    roofline = {
-        "bound": "fp64",
-        "kernel": "fused_kernel<mixed> (flr_fused.cu)",
-        "achieved": idx_ops["total"] * n_out / fused_secs / 1e9,
-        "peak": peak / 1e9,
-        "unit": "G FP64-ops/s",
-        "frac": idx_ops["total"] * n_out / fused_secs / peak,
-        "definition": "FP64 operations the bit-exact delay/index path needs per output "
-                      f"sample (perfmodel.mixed_index_ops: {idx_ops['total']}), over the "
-                      "launch's CUDA-event time; the double-float taps run on the FP32 pipe "
-                      "and are not counted",
-        "peak_source": "measured in this run: FP64 FMA probe kernel (flr_probe_pipe_rate), "
-                       "best of 3; MEASURED_PEAKS.json has no FP64 figure",
-        "launch_ms": fused_ms,
-        "algorithmic_bytes": fused_bytes,
-        "traffic": load_traffic("fused_kernel_mixed", args.workload),
-        "hbm": {"achieved_gbs": fused_bytes / fused_secs / 1e9, "peak_gbs": hbm_peak,
-                "frac": (fused_bytes / fused_secs / 1e9 / hbm_peak) if hbm_peak else None,
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if hbm_peak else None},
-        "pipe_peaks_g_per_s": {k: v / 1e9 for k, v in peaks.items() if k != "sms"},
-    }
-    kern = {k: 1e3 * statistics.mean(a.elapsed_time(b) * 1e-3 for a, b in pev[k])
-            for k in ("response", "tdi")}
-    counts = perfmodel.counts_per_sample(w["order"], tables["num_units"], n_delay_links)
-    computed = {"response": n - 2 * resp.projections_start_ind,
-                "tdi": n - 2 * resp.tdi_start_ind}
-    dominant = max(kern, key=kern.get)
-    c = counts[dominant]
-    slots = perfmodel.fp64_slots(c, div_cost) * computed[dominant]
-    psecs = kern[dominant] * 1e-3
-    plain = {
-        "value": n_out * plain_steps / plain_elapsed,
-        "ms_per_step": 1e3 * plain_elapsed / plain_steps,
-        "steps": plain_steps,
-        "path": "pyResponseTDI.get_projections + get_tdi_delays (two plain FP64 kernels, "
-                "bit-identical to the reference's CPU arithmetic)",
-        "kernels_ms": kern,
-        "roofline": {
-            "bound": "fp64", "kernel": f"{dominant}_plain_kernel",
-            "achieved": slots / psecs / 1e9, "peak": peak / 1e9, "unit": "G FP64-slots/s",
-            "frac": slots / psecs / peak,
-            "frac_division_as_one_op": (c["ops"] + c["divs"]) * computed[dominant] / psecs / peak,
-            "definition": "reference-arithmetic FP64 work (perfmodel.counts_per_sample: "
-                          f"{c['ops']} ops + {c['divs']} divisions per sample for {dominant}), "
-                          f"divisions weighted by their measured cost ({div_cost:.2f} FMA "
-                          "slots)",
-            "traffic": load_traffic(f"{dominant}_plain_kernel", args.workload),
-        },
-    }
+    head = run_headline(args, device, peaks, rank, world)
     result = {
         "metric": METRIC,
-        "value": n_out * args.steps * world / elapsed,
+        "value": head["value"],
         "unit": UNIT,
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": 1e3 * elapsed / args.steps,
+        "ms_per_step": head["ms_per_step"],
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64 delays/indices + double-float (2xf32) taps; outputs f64",
-        "data": "synthetic (seeded galactic-binary waveform, analytic orbits)",
-        "config": {"workload": w["desc"], "name": args.workload, "samples_per_step": n_out,
-                   "input_samples": n,
-                   "path": "mixed-precision fused kernel (BatchedResponseTDI, one source, "
-                           f"{HEADLINE_CHUNKS} tile-aligned launches over two streams per step, "
-                           "the same bits as one launch); integer delay indices bit-exact",
-                   "single_launch_samples_per_s": n_out * max(1, min(args.steps, 5))
-                   / single_elapsed,
-                   "tile": bat.plan_info["tile"], "tile_tuning": bat.tune,
-                   "l2": "flushed before every timed step (256 MB write); h 16 B + XYZ "
-                         f"24 B per sample = {40 * n / 1e6:.0f} MB per step"},
-        "accuracy": {"max_rel_l2_vs_plain_fp64": max_rel, "bound": 1e-6,
-                     "per": "TDI channel, this run's outputs"},
-        "plain_fp64": plain,
-        "speedup_vs_plain_fp64": (n_out * args.steps / elapsed) / plain["value"],
-        "e2e": {"value": n_out * args.steps * world / e2e_elapsed, "unit": UNIT,
-                "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 24 * n,
-                "api": "BatchedResponseTDI.run_host: the input in pinned host memory, X/Y/Z "
-                       "returned to pinned host memory, copies overlapped with the chunks' "
-                       f"launches ({E2E_CHUNKS} chunks, 2 compute streams)"},
-        "gpu_launches": args.steps * HEADLINE_CHUNKS,
-        "roofline": roofline,
-        "clocks": clock_info,
+        "data": "synthetic (seeded galactic binaries generated on the device; analytic "
+                "equal-arm orbits)",
+        "config": batch_config(args.batch_sources),
+        "gpu_launches": head["gpu_launches"],
+        "roofline": head["roofline"],
+        "clocks": head["clocks"],
+        "e2e": head["e2e"],
     }
-    if args.batch_sources > 0:
-        result["batched"] = run_batch_section(args, device, peaks, rank, world)
-    if args.precision_sources > 0 and world == 1:
-        result["precision"] = run_precision_section(args, device)
-    if args.serve_requests > 0 and world == 1:
-        result["serving"] = run_serving_section(args, device)
-    return result
+    if cpu_line is not None:
+        result["cpu_baseline"] = cpu_line
+    details = {}
+    if world == 1:
+        result["single_source"] = run_single_source(args, device, peaks)
+        if args.precision_sources > 0:
+            result["precision"] = run_precision_section(args, device)
+        if args.serve_requests > 0:
+            result["serving"], details["serving"] = run_serving_section(args, device)
+    # the line ends with the comparison on the same sources
+    result["pipe_peaks_g_per_s"] = {k: v / 1e9 for k, v in peaks.items() if k != "sms"}
+    result["plan"] = head["plan"]
+    result["fp64_fused"] = head["fp64_fused"]
+    result["mixed_on_subset"] = head["mixed_on_subset"]
+    result["accuracy"] = head["accuracy"]
+    result["plain_fp64"] = head["plain_fp64"]
+    result["speedup_vs_plain_fp64"] = head["value"] / world / head["plain_fp64"]["value"]
+    return result, details
 
 
-def cpu_baseline_line(args, cores: int, variant: str = "o3"):
-    steps = max(1, min(args.steps, 3))
-    r = cpu_rate(args.workload, cores, steps=steps, warmup=1, variant=variant)
-    w = WORKLOADS[args.workload]
+def cpu_baseline_line(args, cores: int):
+    steps, per_core = 2, 20
+    r = cpu_rate(args.batch_sources, cores, steps=steps, warmup=0, tasks_per_core=per_core)
     return {"value": r["value"], "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{cores} independent source(s) of {CPU_SLICE} samples "
-                      f"({output_samples(CPU_SLICE, w['dt'])} output samples each) in the "
-                      f"workload's configuration, {steps} timed passes; C oracle "
-                      f"(oracle/flr_oracle.c, gcc -O3), one process per core",
+            "sample": f"{steps} x {cores * per_core} slices of {CPU_SLICE} output samples "
+                      "(whole source when shorter) spread over the batch's sources, each with "
+                      "its edge zones; C restatement of the reference's CPU path "
+                      "(oracle/flr_oracle.c, gcc -O3), one process per core",
             "seconds": r["seconds"]}
 
 
 def run_reference(args):
     cores = os.cpu_count() or 1
-    w = WORKLOADS[args.workload]
-    r = cpu_rate(args.workload, cores, steps=args.steps, warmup=args.warmup, variant="o3")
-    line = {
+    r = cpu_rate(args.batch_sources, cores, steps=args.steps, warmup=args.warmup,
+                 tasks_per_core=2)
+    sample = (f"per step {2 * cores} slices of {CPU_SLICE} output samples (whole source when "
+              "shorter) spread over the batch's sources, each with its edge zones")
+    return {
         "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded galactic-binary waveform, analytic orbits)",
-        "config": {"workload": w["desc"], "name": args.workload,
-                   "samples_per_step": r["samples_per_step"],
-                   "cpu_slice": f"{CPU_SLICE} samples per source, one source per core"},
+        "data": "synthetic (seeded galactic binaries; analytic equal-arm orbits)",
+        "config": batch_config(args.batch_sources),
         "impl": "reference",
         "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{cores} sources x {CPU_SLICE} samples per step"},
+                         "sample": sample},
         "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
-        "note": "the reference's CPU path, restated in C (oracle/flr_oracle.c) and pinned "
-                "bit for bit to the reference's own compiled CPU code; the port is timed "
-                "because the reference's code cannot be built without its sources and "
-                "lisaanalysistools, which the GPU host does not have",
+        "note": "the reference's CPU path restated in C (oracle/flr_oracle.c, gcc -O3), pinned "
+                "bit for bit to the reference's own compiled CPU code; the reference's sources "
+                "and lisaanalysistools are not on the GPU host",
     }
-    return line
 
 
 def run_profile_batch(spec: str) -> None:
@@ -875,7 +927,7 @@ def run_profile_batch(spec: str) -> None:
     dev = torch.device("cuda", 0)
     dt, ns, n = 10.0, 16, 2**18
     rng = np.random.default_rng(5)
-    t_max = (n * dt // 1e4 + 3) * 1e4
+    t_max = orbit_t_max(n, dt)
     orb = flr.EqualArmlengthOrbits(t_max=t_max) if kind == "equal" else \
         flr.KeplerianOrbits(t_max=t_max)
     p = flr.waveforms.draw_gb_parameters(rng, ns)
@@ -897,14 +949,15 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--batch-sources", type=int, default=2048,
-                    help="sources in the batching section (0 = skip)")
+    ap.add_argument("--batch-sources", type=int, default=BATCH["sources"],
+                    help="sources of the headline batch (default 2048)")
     ap.add_argument("--serve-requests", type=int, default=1000,
                     help="requests per arrival rate in the serving section (0 = skip)")
     ap.add_argument("--precision-sources", type=int, default=32,
                     help="sources of 2^20 samples in the precision section (0 = skip)")
+    ap.add_argument("--details", default=None, metavar="FILE",
+                    help="also write the serving section's full statistics to FILE")
     ap.add_argument("--profile-batch", default=None, metavar="PREC:ORBIT",
                     help="run only the small batched profiling case (fp64|mixed:equal|kepler)")
     args = ap.parse_args()
@@ -939,10 +992,11 @@ def main():
     torch.cuda.set_device(device)
     if world > 1:
         torch.distributed.init_process_group("nccl", device_id=device)
-    result = run_ours(args, rank, world, device)
-    if cpu_line is not None:
-        result["cpu_baseline"] = cpu_line
+    result, details = run_ours(args, rank, world, device, cpu_line)
     if rank == 0:
+        if args.details:
+            with open(args.details, "w") as fh:
+                json.dump(details, fh, indent=1)
         print(json.dumps(result), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -15,13 +15,13 @@ from .orbits import EqualArmlengthOrbits, KeplerianOrbits, Orbits
 from .serve import Request, ResponseServer
 from .response import (ResponseWrapper, lagrange_tables, pyResponseTDI, sky_basis,
                        tdi_unit_tables)
-from .utils import AET, get_overlap
+from .utils import AET, HostArray, get_overlap
 from .waveforms import GBWave, gb_waveform, time_grid
 
 __version__ = "0.1.0"
 
 __all__ = [
-    "AET", "BatchGraph", "BatchedResponseTDI", "EqualArmlengthOrbits", "FLRError", "GBWave", "KeplerianOrbits",
+    "AET", "BatchGraph", "HostArray", "BatchedResponseTDI", "EqualArmlengthOrbits", "FLRError", "GBWave", "KeplerianOrbits",
     "LISAResponseWrap", "LISAResponseWrapGPU", "Orbits", "OrbitsWrap",
     "OrbitsWrapGPU_responselisa", "ResponseWrapper", "autotune", "build", "describe_status",
     "gb_waveform", "get_overlap", "lagrange_tables", "library_path", "needs_build",

@@ -18,6 +18,7 @@ call (response.py:455-673).
 
 from __future__ import annotations
 
+import collections
 import ctypes
 from typing import Optional, Sequence
 
@@ -349,23 +350,30 @@ class BatchedResponseTDI:
         return inner.view(ns, 2, 3), hs
 
     def run_host(self, h: Sequence, lam, beta, t0=0.0, tdi_set=0, out: Optional[Sequence] = None,
-                 chunks: int = 4):
+                 chunks: int = 4, group_samples: Optional[int] = None):
         """Evaluate sources whose waveforms are in host memory, overlapping the
         host-device copies with the computation.
 
-        Each source's output range is split into ``chunks`` tile-aligned
-        pieces.  A copy stream moves the input in pieces (each with the halo
-        its chunk's delays can reach), two compute streams with a plan each
-        run the chunks (a chunk's tail overlaps the next one's start) and a
-        second copy stream returns each chunk's channels as soon as it is
-        done.  Results are bit-identical to ``__call__`` on device copies of
-        the inputs (sample i is at t0 + i dt in every chunk).
+        The work is cut into launches: with ``group_samples`` set, runs of
+        consecutive sources shorter than it are launched together, about
+        ``group_samples`` samples per launch; every other source's output
+        range is split into ``chunks`` tile-aligned pieces.  A copy stream
+        moves each launch's input (a chunk's with the halo its delays can
+        reach), two compute streams with a plan each run the launches (one
+        launch's tail overlaps the next one's start) and a second copy stream
+        returns each launch's channels as soon as it is done.  Results are
+        bit-identical to ``__call__`` on device copies of the inputs (sample i
+        is at t0 + i dt in every chunk and group).
 
         Args:
-            h: host complex128 waveforms (pinned memory for asynchronous copies).
+            h: host complex128 waveforms (pinned or registered memory for
+                asynchronous copies).
             lam, beta, t0, tdi_set: as for __call__.
             out: optional host (3, n) float64 tensors (pinned); allocated
                 pinned when omitted.
+            chunks: pieces per source launched alone.
+            group_samples: samples per launch of grouped short sources
+                (None: every source is launched alone, in ``chunks`` pieces).
         Returns:
             the list of host output tensors; the current CUDA stream is made to
             wait for them (synchronise it before reading them on the host).
@@ -386,15 +394,43 @@ class BatchedResponseTDI:
             if (tuple(o.shape) != (3, len(x)) or o.dtype != torch.float64
                     or o.device.type != "cpu" or not o.is_contiguous()):
                 raise ValueError(f"out[{i}] must be a contiguous (3, {len(x)}) float64 host tensor")
-        self._pipeline(None, hh, None, outs, lam, beta, t0, sets, chunks, None)
+        self._pipeline(None, hh, None, outs, lam, beta, t0, sets, chunks, None,
+                       group_samples=group_samples)
         return outs
 
+    def _launch_units(self, lengths, chunks, group_samples):
+        """The launches of a pipelined run: lists of (source, output range or
+        None = the whole source).  Consecutive sources shorter than
+        group_samples share launches of about that many samples; the others
+        are launched alone in `chunks` tile-aligned pieces."""
+        tile, ts = self.plan_info["tile"], self.tdi_start_ind
+        units, cur, cur_n = [], [], 0
+        for i, n in enumerate(lengths):
+            if group_samples is not None and n < group_samples:
+                cur.append((i, None))
+                cur_n += n
+                if cur_n >= group_samples:
+                    units.append(cur)
+                    cur, cur_n = [], 0
+                continue
+            if cur:
+                units.append(cur)
+                cur, cur_n = [], 0
+            tiles = -(-(n - 2 * ts) // tile)
+            per = -(-tiles // max(1, min(int(chunks), tiles)))
+            for a in range(0, tiles, per):
+                units.append([(i, (ts + a * tile, min(ts + (a + per) * tile, n - ts)))])
+        if cur:
+            units.append(cur)
+        return units
+
     def _pipeline(self, d_hs, host_hs, d_outs, host_outs, lam, beta, t0, tdi_set, chunks,
-                  stream):
-        """Chunked execution over two compute streams: each source's outputs in
-        `chunks` tile-aligned launches; with host inputs/outputs, a copy stream
-        brings each chunk's input (with the reach of its delays) and another
-        returns its channels.  The calling stream waits for the result."""
+                  stream, group_samples=None):
+        """Pipelined execution over two compute streams (see run_host): the
+        launches of _launch_units alternate between this plan and its twin;
+        with host inputs/outputs, a copy stream brings each launch's input
+        (with the reach of a chunk's delays) and another returns its
+        channels.  The calling stream waits for the result."""
         dev = self.device
         host = host_hs is not None
         ns = len(host_hs if host else d_hs)
@@ -412,50 +448,69 @@ class BatchedResponseTDI:
         start.record(cur)
         for s_ in self._side_streams:
             s_.wait_event(start)
-        tile, ts, reach = self.plan_info["tile"], self.tdi_start_ind, self._reach
-        k = 0
-        for i in range(ns):
-            if host:
-                n = len(host_hs[i])
-                d_h = torch.empty(n, dtype=torch.complex128, device=dev)
-                d_o = torch.empty((3, n), dtype=torch.float64, device=dev)
-                for s_ in self._side_streams:
-                    d_h.record_stream(s_)
-                    d_o.record_stream(s_)
-            else:
-                d_h, d_o = d_hs[i], d_outs[i]
-                n = len(d_h)
+        lengths = [len(x) for x in (host_hs if host else d_hs)]
+        if not host:
+            for i, (d_o, n) in enumerate(zip(d_outs, lengths)):
                 if (tuple(d_o.shape) != (3, n) or d_o.dtype != torch.float64 or not d_o.is_cuda
                         or not d_o.is_contiguous()):
                     raise ValueError(f"out[{i}] must be a contiguous (3, {n}) float64 CUDA tensor")
-            tiles = -(-(n - 2 * ts) // tile)
-            per = -(-tiles // max(1, min(int(chunks), tiles)))
-            ranges = [(ts + a * tile, min(ts + (a + per) * tile, n - ts))
-                      for a in range(0, tiles, per)]
-            done_in = 0
-            for c, (a, b) in enumerate(ranges):
-                last = c == len(ranges) - 1
-                comp = s_comp[k % 2]
-                if host:
-                    need = n if last else min(n, b + reach)
-                    ev_in = torch.cuda.Event()
-                    with torch.cuda.stream(s_in):
-                        if need > done_in:
-                            d_h[done_in:need].copy_(host_hs[i][done_in:need], non_blocking=True)
-                            done_in = need
-                        ev_in.record(s_in)
-                    comp.wait_event(ev_in)
-                plans[k % 2]._run([d_h], None, [n], lam[i:i + 1], beta[i:i + 1], t0[i:i + 1],
-                                  sets[i:i + 1], [d_o], comp, False, None, out_range=(a, b))
-                if host:
-                    ev_k = torch.cuda.Event()
-                    ev_k.record(comp)
-                    s_out.wait_event(ev_k)
-                    lo, hi = (0 if c == 0 else a), (n if last else b)
-                    with torch.cuda.stream(s_out):
-                        for r in range(3):
-                            host_outs[i][r, lo:hi].copy_(d_o[r, lo:hi], non_blocking=True)
-                k += 1
+        reach = self._reach
+        d_h, d_o, done_in = {}, {}, {}
+        in_flight = collections.deque()  # completion events of the launches' returns
+        for k, unit in enumerate(self._launch_units(lengths, chunks, group_samples)):
+            comp = s_comp[k % 2]
+            idx = [i for i, _ in unit]
+            if host:
+                ev_in = torch.cuda.Event()
+                with torch.cuda.stream(s_in):
+                    for i, rng in unit:
+                        n = lengths[i]
+                        if i not in d_h:  # device buffers of a source, made when first needed
+                            d_h[i] = torch.empty(n, dtype=torch.complex128, device=dev)
+                            d_o[i] = torch.empty((3, n), dtype=torch.float64, device=dev)
+                            for s_ in self._side_streams:
+                                d_h[i].record_stream(s_)
+                                d_o[i].record_stream(s_)
+                            done_in[i] = 0
+                        last = rng is None or rng[1] == n - self.tdi_start_ind
+                        need = n if last else min(n, rng[1] + reach)
+                        if need > done_in[i]:
+                            d_h[i][done_in[i]:need].copy_(host_hs[i][done_in[i]:need],
+                                                          non_blocking=True)
+                            done_in[i] = need
+                    ev_in.record(s_in)
+                comp.wait_event(ev_in)
+                hs_u, outs_u = [d_h[i] for i in idx], [d_o[i] for i in idx]
+            else:
+                hs_u, outs_u = [d_hs[i] for i in idx], [d_outs[i] for i in idx]
+            rng = unit[0][1] if len(unit) == 1 else None
+            plans[k % 2]._run(hs_u, None, [lengths[i] for i in idx], lam[idx], beta[idx], t0[idx],
+                              sets[idx], outs_u, comp, False, None, out_range=rng)
+            if host:
+                ev_k = torch.cuda.Event()
+                ev_k.record(comp)
+                s_out.wait_event(ev_k)
+                with torch.cuda.stream(s_out):
+                    for i, r in unit:
+                        n = lengths[i]
+                        if r is None:
+                            host_outs[i].copy_(d_o[i], non_blocking=True)
+                            continue
+                        lo = 0 if r[0] == self.tdi_start_ind else r[0]
+                        hi = n if r[1] == n - self.tdi_start_ind else r[1]
+                        for c in range(3):
+                            host_outs[i][c, lo:hi].copy_(d_o[i][c, lo:hi], non_blocking=True)
+                    ev_back = torch.cuda.Event()
+                    ev_back.record(s_out)
+                # a source's device buffers go back to the allocator once its last
+                # output is on its way (reused after the copy, by record_stream);
+                # at most three launches' buffers are held at a time
+                for i, r in unit:
+                    if r is None or r[1] == lengths[i] - self.tdi_start_ind:
+                        del d_h[i], d_o[i]
+                in_flight.append(ev_back)
+                if len(in_flight) > 3:
+                    in_flight.popleft().synchronize()
         for s_ in (s_out,) if host else tuple(s_comp):
             end = torch.cuda.Event()
             end.record(s_)

@@ -103,3 +103,26 @@ def prefix_shared_subtractions(delay_lists) -> int:
         total += len(cur) - keep
         prev = cur
     return total
+
+
+def mixed_index_ops_grouped(num_groups: int, max_len: int) -> dict:
+    """FP64 operations of the exact index path per output sample in the mixed
+    kernel's equal-arm form, counted as in :func:`mixed_index_ops`: all six
+    light travel times are one value, every link leaving a spacecraft has the
+    same emission time, so a sample needs three receiver sides and three
+    emitter sides (not six links), and the TDI units of one delay-list length
+    share one delay and one index split (`num_groups` lengths, partial sums up
+    to `max_len` links)."""
+    receiver = (1          # segment(t)
+                + 6        # x_rec: 3 coordinates
+                + 6        # k.x_rec
+                + 2        # delay
+                + 6)       # index split
+    emitter = (4           # L(t) (the receiver's segment)
+               + 1 + 1 + 8  # t_em, segment(t_em), x_em
+               + 6         # k.x_em
+               + 2         # delay
+               + 6)        # index split
+    response = 3 * receiver + 3 * emitter
+    tdi = 1 + 2 + max_len + num_groups * 6
+    return {"response": response, "tdi": tdi, "total": response + tdi}

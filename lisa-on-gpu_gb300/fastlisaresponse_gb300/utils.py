@@ -1,9 +1,11 @@
-"""Post-processing helpers of the response path: XYZ -> AET and the overlap
-metric the reference's tests use."""
+"""Helpers of the response path: XYZ -> AET, the overlap metric the
+reference's tests use, and page-locked NumPy host arrays for asynchronous
+host-device copies."""
 
 from __future__ import annotations
 
 import math
+import mmap
 
 import numpy as np
 
@@ -66,3 +68,48 @@ def get_overlap(sig1, sig2, phase_maximize=False, use_gpu=False):
     if phase_maximize:
         return float(abs(overlap))
     return float(np.real(overlap))
+
+
+class HostArray:
+    """A NumPy array in page-locked host memory, made by page-locking an
+    anonymous memory map in place (cudaHostRegister): copies between it and
+    the GPU run asynchronously (``BatchedResponseTDI.run_host``).  The map is
+    page-aligned and its own, so registrations never share a page, and its
+    size is exact (no power-of-two rounding of a caching allocator).  Call
+    :meth:`release` (or use it as a context manager) to unlock it.
+
+    ``HostArray(shape, dtype).array`` is the NumPy view;
+    ``.tensor`` a CPU torch tensor on the same memory."""
+
+    def __init__(self, shape, dtype=np.float64):
+        self.shape = tuple(np.atleast_1d(shape).tolist())
+        self.dtype = np.dtype(dtype)
+        nbytes = int(np.prod(self.shape)) * self.dtype.itemsize
+        self._map = mmap.mmap(-1, max(nbytes, 1))
+        self.array = np.frombuffer(self._map, dtype=self.dtype,
+                                   count=int(np.prod(self.shape))).reshape(self.shape)
+        self._registered = False
+        if nbytes:
+            rc = int(torch.cuda.cudart().cudaHostRegister(self.array.ctypes.data, nbytes, 0))
+            if rc != 0:
+                raise RuntimeError(f"cudaHostRegister failed ({rc})")
+            self._registered = True
+        self.tensor = torch.from_numpy(self.array)
+
+    def release(self):
+        if self._registered:
+            torch.cuda.cudart().cudaHostUnregister(self.array.ctypes.data)
+            self._registered = False
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.release()
+        return False
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass

@@ -1,7 +1,8 @@
 """Host-memory runs (BatchedResponseTDI.run_host): sources split into
-tile-aligned chunks (flr_batch_source.out_begin/out_end), copies overlapped
-with the chunks' launches on two compute streams; the channels equal those of
-a device run bit for bit, edge zones included, for any chunk count."""
+tile-aligned chunks (flr_batch_source.out_begin/out_end) or short sources
+grouped into shared launches, copies overlapped with the launches on two
+compute streams; the channels equal those of a device run bit for bit, edge
+zones included, for any chunk count and grouping."""
 
 import numpy as np
 import pytest
@@ -35,6 +36,44 @@ def test_run_host_matches_device_run(gpu_lib, precision, orbit_kind, chan):
         torch.cuda.synchronize(bat.device)
         for g, w in zip(got, want):
             assert np.array_equal(g.numpy(), w), f"chunks={chunks}"
+    assert bat.status() == 0
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_run_host_groups_short_sources(gpu_lib, precision):
+    """group_samples: runs of short sources share launches (long ones are
+    still chunked), with page-locked NumPy host arrays (HostArray); same
+    bits as one device run."""
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+
+    dt = 10.0
+    orb = flr.EqualArmlengthOrbits(t_max=1.6e6)
+    lengths = [2300, 5000, 41000, 3000, 123457, 9000, 2500, 60001, 4100]
+    hs, lam, beta, t0 = _sources(orb, dt, lengths, seed=47)
+    bat = flr.BatchedResponseTDI(1 / dt, tdi="2nd generation", orbits=orb, precision=precision)
+    want = [_np(o) for o in bat(hs, lam, beta, t0=t0)]
+    h_host = [flr.HostArray(n, np.complex128) for n in lengths]
+    o_host = [flr.HostArray((3, n)) for n in lengths]
+    for a, x in zip(h_host, hs):
+        a.array[:] = np.asarray(x)
+    try:
+        units = bat._launch_units(lengths, 3, 50000)
+        assert sorted(i for u in units for i, r in u if r is None or r[0] == bat.tdi_start_ind) \
+            == list(range(len(lengths)))
+        assert any(len(u) > 1 for u in units)
+        for group in (50000, 10**9):
+            for o in o_host:
+                o.array.fill(np.nan)
+            got = bat.run_host([a.tensor for a in h_host], lam, beta, t0=t0,
+                               out=[o.tensor for o in o_host], chunks=3, group_samples=group)
+            torch.cuda.synchronize(bat.device)
+            for g, w in zip(got, want):
+                assert np.array_equal(g.numpy(), w), f"group_samples={group}"
+    finally:
+        for a in h_host + o_host:
+            a.release()
     assert bat.status() == 0
 
 

@@ -45,3 +45,13 @@ def test_prefix_sharing_and_bytes():
     assert pm.prefix_shared_subtractions([[12], [12, 21], [13], [13, 31, 12]]) == 1 + 1 + 1 + 2
     assert pm.prefix_shared_subtractions([]) == 0
     assert pm.BYTES_PER_SAMPLE == {"response": 64, "tdi": 72, "total": 136}
+
+
+def test_mixed_index_path_counts_equal_arms():
+    """Equal arms: three receiver and three emitter sides per sample, one
+    split per delay-list length (8 lengths up to 7 links in 2nd generation)."""
+    _, _, lists = _tables(2)
+    lens = {len(x) for x in lists}
+    assert (len(lens), max(lens)) == (8, 7)
+    got = pm.mixed_index_ops_grouped(len(lens), max(lens))
+    assert got == {"response": 3 * 21 + 3 * 28, "tdi": 3 + 7 + 48, "total": 205}
