@@ -175,6 +175,18 @@ int flr_tdi_delay_indices(flr_orbits *orbits, int *d_tdi, int num_delays, const 
                           double sampling_frequency, int tdi_start_ind, void *stream);
 
 /*
+ * A, E (and T) from X, Y, Z as lisaanalysistools' AET defines them:
+ * (Z - X)/sqrt2, (X - 2Y + Z)/sqrt6, (X + Y + Z)/sqrt3, in NumPy's operation
+ * order with correctly rounded division, for the samples [start,
+ * num_delays - start) of channel-major rows (xyz [3][num_delays] in, aet
+ * [num_rows][num_delays] out, num_rows 3 for AET or 2 for AE; other samples
+ * untouched).  Replaces the reference's call of lisatools' AET on the TDI
+ * output (response.py:659-673), which is host Python in the reference.
+ */
+int flr_xyz_to_aet(const double *xyz, double *aet, int num_delays, int start, int num_rows,
+                   void *stream);
+
+/*
  * ------------------------------------------------------------------------
  * Batched, fused response + TDI (no reference counterpart: the reference
  * evaluates one source per call, with two launches and a device
@@ -261,13 +273,16 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
                           const flr_tdi_units *sets, int num_sets, int precision, int tile,
                           flr_batch_plan **out);
 int flr_batch_plan_destroy(flr_batch_plan *plan);
-/* info[0..8] = tile, y halo, input window capacity, link row capacity, shared
+/* info[0..9] = tile, y halo, input window capacity, link row capacity, shared
  * memory bytes per block, persistent grid size, precision, 1 when the mixed
  * kernel evaluates the TDI units in equal-delay groups (equal-arm orbits:
  * units with delay lists of equal length share one interpolation of their
- * combined link rows), and the first outer tap j of the TDI interpolations
- * that the mixed kernel evaluates in FP32 (its weights are small enough; the
- * half-width h when none). */
+ * combined link rows), the first outer tap j of the TDI interpolations that
+ * the mixed kernel's double-float form evaluates in FP32 (its weights are
+ * small enough; the half-width h when none), and 1 when the mixed kernel
+ * evaluates the TDI interpolations in second-difference form (a double-float
+ * linear part plus an FP32 sum over second differences; needs the reference's
+ * Lagrange tables, else the double-float form is used). */
 int flr_batch_plan_info(const flr_batch_plan *plan, int *info, int n_info);
 
 /* Test hook (no reference counterpart): the bound, in mbarrier polls, of each

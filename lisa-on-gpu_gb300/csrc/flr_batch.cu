@@ -163,6 +163,83 @@ void make_groups(flr::FusedTdiSet &s) {
     s.grouped = 1;
 }
 
+// The second-difference form of the mixed kernel's TDI interpolation needs
+// S(eps) = lerp(A)(eps) / A_exact(eps), the ratio of the caller's A table
+// (linearly interpolated, as the reference does) to the exact Lagrange
+// prefactor A_exact(eps) = prod_{i=1}^{h-1} (i + eps)(i + 1 - eps) / ((h-1)! h!)
+// of which the table is a sampling.  Per table segment [a deps, (a+1) deps]
+// the deviation sigma = S - 1 (|sigma| <= ~2e-7, zero at the knots) is a
+// smooth function of u = eps / deps - a, stored as a degree-4 polynomial in u
+// with FP32 coefficients (c4, c3, c2, c1) and c0.  Fitted at five Chebyshev
+// nodes in long double and checked at 17 points as the kernel evaluates it:
+// false (the form is not used) when it misses sigma by more than 1e-13
+// anywhere (the FP32 coefficients alone carry ~1e-14), or when the E table
+// does not hold the weights whose sum is 1 / A_exact (a table other than the
+// reference's).
+bool fit_sigma_table(const std::vector<double> &A, const std::vector<double> &E, int h,
+                     double deps, std::vector<float4> &c4, std::vector<float> &c0) {
+    const int segs = (int)A.size() - 1;
+    if (segs < 1 || h < 2) return false;
+    long double fact_h1 = 1.0L;
+    for (int i = 2; i <= h - 1; ++i) fact_h1 *= i;
+    const long double fact_h = fact_h1 * h;
+    auto a_exact = [&](long double e) {
+        long double p = 1.0L;
+        for (int i = 1; i < h; ++i) p *= (i + e) * (i + 1 - e);
+        return p / (fact_h1 * fact_h);
+    };
+    // the unnormalised weights (1 - e, e, e (1 - e) E_j / (j + e), e (1 - e) E_j / (j + 1 - e))
+    // must sum to 1 / A_exact
+    for (int k = 1; k < 8; ++k) {
+        const long double e = k / 8.0L;
+        long double tail = 0.0L;
+        for (int j = 1; j < h; ++j) tail += E[j - 1] * (1.0L / (j + e) + 1.0L / (j + 1 - e));
+        const long double sum = 1.0L + e * (1 - e) * tail;
+        if (std::fabs((double)(sum * a_exact(e) - 1.0L)) > 1e-13) return false;
+    }
+    c4.resize(segs);
+    c0.resize(segs);
+    constexpr int m = 5;
+    long double node[m];
+    for (int i = 0; i < m; ++i)
+        node[i] = 0.5L - 0.5L * std::cos((2 * i + 1) * 3.14159265358979323846L / (2 * m));
+    for (int a = 0; a < segs; ++a) {
+        auto sigma = [&](long double u) {
+            const long double lerp = A[a] + u * ((long double)A[a + 1] - (long double)A[a]);
+            return lerp / a_exact((a + u) * (long double)deps) - 1.0L;
+        };
+        // Vandermonde system V c = sigma(node), c = (c0 .. c4), Gauss-Jordan elimination
+        long double V[m][m + 1];
+        for (int i = 0; i < m; ++i) {
+            long double pw = 1.0L;
+            for (int j = 0; j < m; ++j, pw *= node[i]) V[i][j] = pw;
+            V[i][m] = sigma(node[i]);
+        }
+        for (int col = 0; col < m; ++col) {
+            int piv = col;
+            for (int r = col + 1; r < m; ++r)
+                if (std::fabs((double)V[r][col]) > std::fabs((double)V[piv][col])) piv = r;
+            for (int j = 0; j <= m; ++j) std::swap(V[col][j], V[piv][j]);
+            for (int r = 0; r < m; ++r) {
+                if (r == col) continue;
+                const long double f = V[r][col] / V[col][col];
+                for (int j = col; j <= m; ++j) V[r][j] -= f * V[col][j];
+            }
+        }
+        float c[m];
+        for (int j = 0; j < m; ++j) c[j] = (float)(V[j][m] / V[j][j]);
+        for (int k = 0; k <= 16; ++k) {  // the FP32 polynomial as the kernel evaluates it
+            const float u = k / 16.0f;
+            const float v = std::fma(std::fma(std::fma(std::fma(c[4], u, c[3]), u, c[2]), u, c[1]),
+                                     u, c[0]);
+            if (std::fabs((double)((long double)v - sigma(u))) > 1e-13) return false;
+        }
+        c4[a] = make_float4(c[4], c[3], c[2], c[1]);
+        c0[a] = c[0];
+    }
+    return true;
+}
+
 // Staging layout: descriptors | tile prefix sums | waveform parameters |
 // chunk prefix sums, each part 256-byte aligned.
 struct StageLayout {
@@ -293,7 +370,12 @@ cudaError_t enqueue(const flr_batch_plan *plan, const unsigned char *h_stage,
     a.num_sources = cap;
     a.chan = chan;
     a.partial = partial;
-    err = flr::launch_fused(plan->mixed, plan->grouped, diag, partial != nullptr, a, plan->grid_max,
+    // the difference forms for XYZ outputs; AET / AE keep the double-float form,
+    // whose absolute error stays ~1e-14 of the links: those channels are
+    // combinations of X, Y, Z that can cancel to a small fraction of them
+    const bool d2 = plan->mixed && plan->base.d2 && chan == FLR_CHAN_XYZ;
+    err = flr::launch_fused(plan->mixed, plan->grouped, diag, partial != nullptr, d2, a,
+                            plan->grid_max,
                             plan->smem, st);
     if (err == cudaSuccess && partial) err = flr::launch_inner_reduce(a, st);
     return err;
@@ -454,7 +536,9 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
     const size_t a_bytes = sizeof(double) * (size_t)num_A;
     const size_t e_bytes = sizeof(double) * (size_t)std::max(h - 1, 1);
     const size_t atab_off = (a_bytes + e_bytes + 255) & ~size_t(255);
-    const size_t set_off = (atab_off + sizeof(float4) * (size_t)num_A + 255) & ~size_t(255);
+    const size_t sig4_off = (atab_off + sizeof(float4) * (size_t)num_A + 255) & ~size_t(255);
+    const size_t sig0_off = (sig4_off + sizeof(float4) * (size_t)num_A + 255) & ~size_t(255);
+    const size_t set_off = (sig0_off + sizeof(float) * (size_t)num_A + 255) & ~size_t(255);
     std::vector<double> a_host(num_A);
     err = cudaMemcpy(a_host.data(), A_in, a_bytes, cudaMemcpyDefault);
     if (err != cudaSuccess) {
@@ -476,7 +560,17 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
         const float ah = (float)a, dah = (float)da;
         a_tab[i] = make_float4(ah, (float)(a - (double)ah), dah, (float)(da - (double)dah));
     }
+    // second-difference TDI form (mixed flavour): the sigma table of the A table
+    std::vector<float4> sig4;
+    std::vector<float> sig0;
+    const bool d2 = mixed && fit_sigma_table(a_host, e_host, h, deps, sig4, sig0);
     err = cudaMalloc(&p->d_tables, set_off + sizeof(flr::FusedTdiSet) * num_sets);
+    if (err == cudaSuccess && d2)
+        err = cudaMemcpy(static_cast<char *>(p->d_tables) + sig4_off, sig4.data(),
+                         sizeof(float4) * sig4.size(), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess && d2)
+        err = cudaMemcpy(static_cast<char *>(p->d_tables) + sig0_off, sig0.data(),
+                         sizeof(float) * sig0.size(), cudaMemcpyHostToDevice);
     if (err == cudaSuccess)
         err = cudaMemcpy(static_cast<char *>(p->d_tables) + atab_off, a_tab.data(),
                          sizeof(float4) * (size_t)num_A, cudaMemcpyHostToDevice);
@@ -547,6 +641,9 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
                                                        set_off);
     b.num_sets = num_sets;
     b.a_tab = reinterpret_cast<const float4 *>(static_cast<char *>(p->d_tables) + atab_off);
+    b.d2 = d2 ? 1 : 0;
+    b.sig4 = reinterpret_cast<const float4 *>(static_cast<char *>(p->d_tables) + sig4_off);
+    b.sig0 = reinterpret_cast<const float *>(static_cast<char *>(p->d_tables) + sig0_off);
     b.wait_polls = flr::kFusedWaitPolls;
     b.fs = sampling_frequency;
     b.dt = 1.0 / sampling_frequency;
@@ -588,7 +685,7 @@ int flr_batch_plan_info(const flr_batch_plan *plan, int *info, int n_info) {
     const int vals[] = {plan->base.tile, plan->base.y_halo, plan->base.win_max,
                         plan->base.y_max, (int)plan->smem, plan->grid_max,
                         plan->mixed ? FLR_PRECISION_MIXED : FLR_PRECISION_FP64,
-                        plan->grouped ? 1 : 0, plan->base.h_df};
+                        plan->grouped ? 1 : 0, plan->base.h_df, plan->base.d2};
     for (int i = 0; i < n_info && i < (int)(sizeof(vals) / sizeof(int)); ++i) info[i] = vals[i];
     return FLR_OK;
 }

@@ -319,4 +319,16 @@ int flr_tdi_delay_indices(flr_orbits *orbits, int *d_tdi, int num_delays, const 
     return FLR_OK;
 }
 
+int flr_xyz_to_aet(const double *xyz, double *aet, int num_delays, int start, int num_rows,
+                   void *stream) {
+    g_last_error.clear();
+    if (!xyz || !aet) return fail(FLR_E_INVALID_ARGUMENT, "array arguments must not be NULL");
+    if (num_delays < 1 || start < 0 || (num_rows != 2 && num_rows != 3))
+        return fail(FLR_E_INVALID_ARGUMENT, "need num_delays >= 1, start >= 0, num_rows 2 or 3");
+    cudaError_t err = flr::launch_xyz_to_aet(xyz, aet, num_delays, start, num_rows,
+                                             static_cast<cudaStream_t>(stream));
+    if (err != cudaSuccess) return cuda_fail(err, "launching the AET kernel");
+    return FLR_OK;
+}
+
 }  // extern "C"

@@ -106,6 +106,13 @@ struct FusedArgs {
     int num_sets;
     const float4 *a_tab;       // per A-table knot: (A hi, A lo, dA hi, dA lo), dA = A[k+1]-A[k]
     int h_df;                  // mixed TDI taps: j < h_df in double-float, the outer ones in FP32
+    // Difference forms of the mixed interpolations available (d2 = 1; the
+    // launch chooses them for XYZ outputs): per A-table segment, sigma(u) =
+    // lerp(A)/A_exact - 1 = ((((c4 u + c3) u + c2) u + c1) u + c0 with
+    // (c4, c3, c2, c1) = sig4[segment] and c0 = sig0[segment]
+    int d2;
+    const float4 *sig4;
+    const float *sig0;
     int tile;                  // output samples per work item
     int y_halo;                // link-stream samples computed before a tile
     int y_halo_hi;             // and after it: TDI delays only look back, so the taps
@@ -149,9 +156,11 @@ cudaError_t fused_configure(bool mixed, bool grouped, size_t smem_bytes, int *bl
 // its inner[6] (sources without inner are skipped).
 cudaError_t launch_inner_reduce(const FusedArgs &a, cudaStream_t stream);
 // diag: the instance that writes the FusedSource diagnostics (more registers);
-// inner: the instance that forms inner products (FusedArgs::partial set).
-cudaError_t launch_fused(bool mixed, bool grouped, bool diag, bool inner, const FusedArgs &a,
-                         int grid, size_t smem_bytes,
-                         cudaStream_t stream);
+// inner: the instance that forms inner products (FusedArgs::partial set);
+// d2: the mixed instance in difference form (FusedArgs::d2 tables required).
+cudaError_t launch_fused(bool mixed, bool grouped, bool diag, bool inner, bool d2,
+                         const FusedArgs &a, int grid, size_t smem_bytes, cudaStream_t stream);
+// The difference-form mixed instances (flr_fused_d2.cu).
+const void *fused_fn_d2(bool grouped, bool diag, bool inner);
 
 }  // namespace flr

@@ -66,6 +66,8 @@ cudaError_t launch_tdi_indices(const TdiArgs &a, int *d_out, cudaStream_t stream
 // Sets the text flr_last_error() returns on the calling thread.
 void set_last_error(const std::string &msg);
 
+cudaError_t launch_xyz_to_aet(const double *xyz, double *aet, long n, long start, int rows,
+                              cudaStream_t stream);
 cudaError_t launch_orbit_slopes(const double *tab, double *slope, long n, int stride, double dt,
                                 cudaStream_t stream);
 

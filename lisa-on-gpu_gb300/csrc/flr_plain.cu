@@ -3,10 +3,13 @@
 // Compiled with --fmad=false (see flr_device.cuh): these kernels reproduce the
 // reference's CPU arithmetic bit for bit.  Parallel layout:
 //
-//   response: one thread per (sample, link); grid (ceil(n/256), 6).  Each
+//   response: one thread per (sample, link); a 1-D grid of ceil(n/256) * 6
+//             blocks, the six links of a 256-sample tile in consecutive blocks
+//             (they read the same input window, which L2 then serves).  Each
 //             thread evaluates the geometry of its link at its sample and the
 //             two complex Lagrange interpolations (LISAResponse.cu:431-672).
-//   TDI:      one thread per (sample, channel); grid (ceil(n/256), channels).
+//   TDI:      one thread per (sample, channel); the channels of a tile in
+//             consecutive blocks likewise (they read the same link windows).
 //             The thread walks the units of its channel in unit order and
 //             accumulates into a register, so the sum order is that of the
 //             reference's CPU loop (LISAResponse.cu:300-396) and deterministic
@@ -34,8 +37,8 @@ __device__ __forceinline__ double quiet_nan() {
 
 __global__ void __launch_bounds__(kThreads)
 response_plain_kernel(ResponseArgs a) {
-    const int slot = blockIdx.y;
-    const long i = (long)a.start + (long)blockIdx.x * kThreads + threadIdx.x;
+    const int slot = (int)(blockIdx.x % kLinks);
+    const long i = (long)a.start + (long)(blockIdx.x / kLinks) * kThreads + threadIdx.x;
     if (i >= a.num_delays - a.start) return;
 
     const double k[3] = {__ldg(a.k), __ldg(a.k + 1), __ldg(a.k + 2)};
@@ -75,8 +78,9 @@ response_plain_kernel(ResponseArgs a) {
 
 __global__ void __launch_bounds__(kThreads)
 tdi_plain_kernel(TdiArgs a) {
-    const int channel = blockIdx.y;
-    const long i = (long)a.start + (long)blockIdx.x * kThreads + threadIdx.x;
+    const int channel = (int)(blockIdx.x % (unsigned)a.num_channels);
+    const long i =
+        (long)a.start + (long)(blockIdx.x / (unsigned)a.num_channels) * kThreads + threadIdx.x;
     if (i >= a.num_delays - a.start) return;
 
     const double t = __ldg(a.t_arr + i);
@@ -182,19 +186,38 @@ dim3 sample_grid(long count, int rows) {
     return dim3((unsigned)((count + kThreads - 1) / kThreads), (unsigned)rows);
 }
 
+// 1-D grid: the `rows` rows of a tile in consecutive blocks
+unsigned interleaved_grid(long count, int rows) {
+    return (unsigned)(((count + kThreads - 1) / kThreads) * rows);
+}
+
+// XYZ -> lisaanalysistools' AET, (Z - X)/sqrt2, (X - 2Y + Z)/sqrt6,
+// (X + Y + Z)/sqrt3, in NumPy's operation order with correctly rounded
+// division (the values of the reference's AET on the same XYZ); `rows` = 2
+// writes A and E only.
+__global__ void __launch_bounds__(kThreads)
+xyz_to_aet_kernel(const double *xyz, double *aet, long n, long start, int rows) {
+    const long i = start + (long)blockIdx.x * kThreads + threadIdx.x;
+    if (i >= n - start) return;
+    const double X = xyz[i], Y = xyz[n + i], Z = xyz[2 * n + i];
+    aet[i] = (Z - X) / 1.4142135623730951;
+    aet[n + i] = (X - 2.0 * Y + Z) / 2.449489742783178;
+    if (rows > 2) aet[2 * n + i] = (X + Y + Z) / 1.7320508075688772;
+}
+
 }  // namespace
 
 cudaError_t launch_response_plain(const ResponseArgs &a, cudaStream_t stream) {
     long count = a.num_delays - 2L * a.start;
     if (count <= 0) return cudaSuccess;
-    response_plain_kernel<<<sample_grid(count, kLinks), kThreads, 0, stream>>>(a);
+    response_plain_kernel<<<interleaved_grid(count, kLinks), kThreads, 0, stream>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_tdi_plain(const TdiArgs &a, cudaStream_t stream) {
     long count = a.num_delays - 2L * a.start;
     if (count <= 0 || a.num_channels <= 0) return cudaSuccess;
-    tdi_plain_kernel<<<sample_grid(count, a.num_channels), kThreads, 0, stream>>>(a);
+    tdi_plain_kernel<<<interleaved_grid(count, a.num_channels), kThreads, 0, stream>>>(a);
     return cudaGetLastError();
 }
 
@@ -210,6 +233,15 @@ cudaError_t launch_tdi_indices(const TdiArgs &a, int *d_out, cudaStream_t stream
     long count = a.num_delays - 2L * a.start;
     if (count <= 0 || a.num_units <= 0) return cudaSuccess;
     tdi_indices_kernel<<<sample_grid(count, a.num_units), kThreads, 0, stream>>>(a, d_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_xyz_to_aet(const double *xyz, double *aet, long n, long start, int rows,
+                              cudaStream_t stream) {
+    const long count = n - 2 * start;
+    if (count <= 0) return cudaSuccess;
+    xyz_to_aet_kernel<<<(unsigned)((count + kThreads - 1) / kThreads), kThreads, 0, stream>>>(
+        xyz, aet, n, start, rows);
     return cudaGetLastError();
 }
 

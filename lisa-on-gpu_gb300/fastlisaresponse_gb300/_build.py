@@ -34,6 +34,7 @@ SOURCES = {
     "flr_capi.cu": [],
     "flr_noalloc.cu": ["--fmad=false"],
     "flr_fused.cu": ["--fmad=false"],
+    "flr_fused_d2.cu": ["--fmad=false"],
     "flr_batch.cu": [],
     "flr_waveform.cu": ["--fmad=false"],
 }

@@ -209,10 +209,11 @@ class BatchedResponseTDI:
         _lib.check(rc)
         self._plan = plan
         self._graphs = {}
-        info = (ctypes.c_int * 9)()
-        lib.flr_batch_plan_info(plan, info, 9)
+        info = (ctypes.c_int * 10)()
+        lib.flr_batch_plan_info(plan, info, 10)
         self.plan_info = dict(zip(("tile", "y_halo", "win_max", "y_max", "smem_bytes",
-                                   "grid", "precision", "grouped", "fp32_tap_from"),
+                                   "grid", "precision", "grouped", "fp32_tap_from",
+                                   "tdi_second_differences"),
                                   list(info)))
         self._ctor = dict(sampling_frequency=sampling_frequency, order=order, tdi=tdi,
                           orbits=orbits, tdi_chan=tdi_chan, precision=precision,
@@ -397,6 +398,49 @@ class BatchedResponseTDI:
         self._pipeline(None, hh, None, outs, lam, beta, t0, sets, chunks, None,
                        group_samples=group_samples)
         return outs
+
+    def run_time_shard(self, h, lam, beta, rank: int, world: int, t0=0.0, tdi_set=0,
+                       stream=None):
+        """One long source sharded by time over `world` ranks (one GPU each):
+        this rank's tile-aligned share of the output samples
+        (:func:`fastlisaresponse_gb300.dist.shard_time`), computed from the
+        slice of the input its delays reach (:func:`dist.input_range`).
+
+        Args:
+            h: the whole complex128 waveform (host or device); only the
+                rank's input slice is read and copied to this GPU (the rest of
+                the device buffer holds NaN, so a read outside the slice would
+                show in the output).
+            lam, beta, t0, tdi_set: as for __call__ (one source).
+            rank, world: this rank and the number of ranks.
+        Returns:
+            (out, out_range, in_range): a (3, n) float64 device tensor whose
+            samples [out_range) are this rank's channels (the first rank's
+            also the zeros before tdi_start, the last rank's those after
+            n - tdi_start; other samples NaN), the output range (None: no
+            tile for this rank) and the input slice read.  The ranks' output
+            ranges partition the output, each sample computed as in a
+            single run (the same bits).
+        """
+        from .dist import input_range, shard_time
+
+        dev = self.device
+        x = torch.as_tensor(h)
+        if x.dtype != torch.complex128 or x.ndim != 1:
+            raise ValueError("h must be a 1-D complex128 array")
+        n = len(x)
+        ts = self.tdi_start_ind
+        out = torch.full((3, n), float("nan"), dtype=torch.float64, device=dev)
+        rng = shard_time(n, ts, self.plan_info["tile"], rank, world)
+        if rng is None:
+            return out, None, None
+        lo, hi = input_range(rng, n, self._reach)
+        d_h = torch.full((n,), complex(float("nan"), float("nan")), dtype=torch.complex128,
+                         device=dev)
+        d_h[lo:hi].copy_(x[lo:hi], non_blocking=x.device.type == "cpu" and x.is_pinned())
+        self._run([d_h], None, [n], lam, beta, t0, tdi_set, [out], stream, False, None,
+                  out_range=rng)
+        return out, rng, (lo, hi)
 
     def _launch_units(self, lengths, chunks, group_samples):
         """The launches of a pipelined run: lists of (source, output range or

@@ -34,7 +34,6 @@ except ImportError:  # pragma: no cover
 from . import _lib
 from .binding import LISAResponseWrap, OrbitsWrap
 from .orbits import EqualArmlengthOrbits, Orbits
-from .utils import AET
 
 YRSID_SI = 31558149.763545603
 C_inv = 3.3356409519815204e-09  # response.py:36
@@ -453,8 +452,14 @@ class pyResponseTDI:
         if self.tdi_chan == "XYZ":
             return X, Y, Z
         if self.tdi_chan in ("AET", "AE"):
-            A, E, T = AET(X, Y, Z)
-            return (A, E, T) if self.tdi_chan == "AET" else (A, E)
+            # lisatools' AET (response.py:659-673) in one kernel: the same values
+            rows = 3 if self.tdi_chan == "AET" else 2
+            aet = torch.zeros((rows, self.num_pts), dtype=torch.float64, device=dev)
+            with torch.cuda.device(dev):
+                _lib.check(_lib.lib().flr_xyz_to_aet(
+                    self.delayed_links_flat.data_ptr(), aet.data_ptr(), self.num_pts,
+                    self.tdi_start_ind, rows, torch.cuda.current_stream(dev).cuda_stream))
+            return tuple(aet[r] for r in range(rows))
         raise ValueError("tdi_chan must be 'XYZ', 'AET' or 'AE'.")
 
     def status(self, reset: bool = False) -> int:

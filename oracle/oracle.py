@@ -53,14 +53,19 @@ _libs: dict = {}
 
 def load(variant: str = "parity") -> ctypes.CDLL:
     """Load the oracle library; ``variant`` is "parity" (-O2, no FP contraction,
-    bit-exact) or "o3" (-O3, used only for CPU-baseline timing)."""
-    name = {"parity": "liboracle.so", "o3": "liboracle_o3.so"}[variant]
+    bit-exact), "o3" (-O3, the CPU-baseline timing build) or "native" (-O3
+    -march=native, for comparing with the reference's own build flags)."""
+    name = {"parity": "liboracle.so", "o3": "liboracle_o3.so",
+            "native": "liboracle_native.so"}[variant]
     if name in _libs:
         return _libs[name]
     path = os.path.join(HERE, name)
     src = os.path.join(HERE, "flr_oracle.c")
     if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
-        build()
+        if variant == "native":
+            subprocess.run(["make", "-s", "-C", HERE, "liboracle_native.so"], check=True)
+        else:
+            build()
     lib = ctypes.CDLL(path)
     dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
     lib.orc_get_response.restype = None

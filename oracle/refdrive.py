@@ -51,6 +51,10 @@ def _reference_root() -> str:
 REF_ROOT = _reference_root()
 REF_PKG = os.path.join(REF_ROOT, "src", "fastlisaresponse")
 REF_LIB = os.path.join(HERE, "_ref", "libflr_ref.so")
+# build of the reference's code ref_lib() loads: "parity" (-O2
+# -ffp-contract=off, the pinning build) or the timing builds "o3" / "native"
+REF_VARIANTS = {"parity": ("ref", "libflr_ref.so"), "o3": ("timing", "libflr_ref_o3.so"),
+                "native": ("timing", "libflr_ref_native.so")}
 
 
 def available() -> bool:
@@ -58,6 +62,16 @@ def available() -> bool:
 
 
 _lib = None
+_variant = "parity"
+
+
+def use_variant(name: str) -> None:
+    """Select the build of the reference's code that later calls use."""
+    global _lib, _variant
+    if name not in REF_VARIANTS:
+        raise ValueError(f"variant must be one of {sorted(REF_VARIANTS)}")
+    if name != _variant:
+        _variant, _lib = name, None
 
 
 def ref_lib() -> ctypes.CDLL:
@@ -66,9 +80,10 @@ def ref_lib() -> ctypes.CDLL:
         return _lib
     if not available():
         raise RuntimeError("the reference sources are not available here")
-    subprocess.run(["make", "-s", "-C", HERE, "ref",
+    target, fname = REF_VARIANTS[_variant]
+    subprocess.run(["make", "-s", "-C", HERE, target,
                     f"REF_DIR={os.path.join(REF_PKG, 'cutils')}"], check=True)
-    lib = ctypes.CDLL(REF_LIB)
+    lib = ctypes.CDLL(os.path.join(HERE, "_ref", fname))
     d, i, p = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
     orb = [d, i, p, p, p, p, p, p, d]
     lib.flr_ref_get_response.argtypes = orb + [p, p, p, p, p, d, i, p, i, i, d, i, p, d, i, p, i]
