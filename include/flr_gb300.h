@@ -297,16 +297,30 @@ int flr_batch_plan_set_wait_limit(flr_batch_plan *plan, long long polls);
 int flr_batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int num_sources,
                   int chan, void *stream);
 
-/* Galactic-binary parameters: h+ = A(1+cos^2 iota) cos Phi, hx = -2A cos iota
- * sin Phi, Phi = phi0 + 2 pi (f t + fdot t^2 / 2), rotated by the polarisation
- * angle psi (hp cos2psi - hx sin2psi, hp sin2psi + hx cos2psi). */
+/* Galactic-binary parameters of a source whose waveform the library
+ * generates (FP64, CUDA's sincos; t = t0 + i / fs), in one of two models:
+ *   FLR_GB_MODEL_CONFIG (0): Phi = phi0 + 2 pi (f t + fdot t^2 / 2),
+ *     h+ = A (1 + cos^2 iota) cos Phi, hx = -2 A cos iota sin Phi;
+ *   FLR_GB_MODEL_GBWAVE (1): the reference test-suite's generator
+ *     (tests/test_fastlisaresponse.py:34-63): fddot = 11/3 fdot^2 / f,
+ *     Phi = 2 pi (f t + fdot t^2 / 2 + fddot t^3 / 6) - phi0,
+ *     h+ = -A (1 + cos^2 iota) cos Phi, hx = -2 A cos iota sin Phi;
+ * both rotated by the polarisation angle psi (h+ cos2psi - hx sin2psi,
+ * h+ sin2psi + hx cos2psi).  Zero-initialised fields select model 0. */
+#define FLR_GB_MODEL_CONFIG 0
+#define FLR_GB_MODEL_GBWAVE 1
 typedef struct {
     double A, f, fdot, iota, phi0, psi;
+    int model;
+    int reserved;
 } flr_gb_params;
 
-/* As flr_batch_run, but first generates each source's waveform on the device
- * into sources[i].h (a device buffer of n complex128 the caller provides) at
- * t_i = t0 + i / fs.  One waveform launch and one fused launch per call. */
+/* As flr_batch_run, with each source's waveform generated on the device at
+ * t_i = t0 + i / fs: into sources[i].h when it is set (a device buffer of n
+ * complex128 the caller provides; one waveform launch writes it, the fused
+ * launch reads it), or, when sources[i].h is NULL, straight into the fused
+ * kernel's staged input window, so that the waveform never reaches memory
+ * (per output sample 24 B of HBM traffic: the channels). */
 int flr_batch_run_gb(flr_batch_plan *plan, const flr_batch_source *sources,
                      const flr_gb_params *params, int num_sources, int chan, void *stream);
 

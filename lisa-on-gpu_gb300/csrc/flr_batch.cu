@@ -274,14 +274,18 @@ int fill_stage(const flr_batch_plan *plan, const flr_batch_source *sources, int 
     *inner = false;
     for (int i = 0; i < num_sources; ++i) {
         const flr_batch_source &s = sources[i];
-        if (!s.h || (!s.out && !s.inner) || s.n < 2 || s.projections_start < 0 ||
+        if ((!s.h && !gb) || (!s.out && !s.inner) || s.n < 2 || s.projections_start < 0 ||
             s.tdi_start < s.projections_start || 2LL * s.tdi_start >= s.n ||
             s.n > (1LL << 31) - 1 || s.tdi_set < 0 || s.tdi_set >= plan->num_sets)
             return fail(FLR_E_INVALID_ARGUMENT,
                         "source " + std::to_string(i) +
-                            ": need h, out (or inner), 0 <= projections_start <= tdi_start "
+                            ": need h (or waveform parameters), out (or inner), "
+                            "0 <= projections_start <= tdi_start "
                             "< n/2, "
                             "n < 2^31 and a valid tdi_set");
+        if (gb && (gb[i].model < 0 || gb[i].model > 1))
+            return fail(FLR_E_INVALID_ARGUMENT,
+                        "source " + std::to_string(i) + ": unknown waveform model");
         if (reinterpret_cast<uintptr_t>(s.h) % 16 != 0)
             return fail(FLR_E_INVALID_ARGUMENT, "source " + std::to_string(i) +
                                                     ": h (complex128) must be 16-byte aligned");
@@ -328,7 +332,8 @@ int fill_stage(const flr_batch_plan *plan, const flr_batch_source *sources, int 
         if (gb) {
             chunk_start[i] = chunks;
             chunks += flr::gb_waveform_chunks((long)s.n);
-            flr::GbParams g{gb[i].A, gb[i].f, gb[i].fdot, gb[i].iota, gb[i].phi0, gb[i].psi};
+            flr::GbParams g{gb[i].A,    gb[i].f,   gb[i].fdot,  gb[i].iota,
+                            gb[i].phi0, gb[i].psi, gb[i].model, 0};
             std::memcpy(reinterpret_cast<flr::GbParams *>(hs + lay.gb) + i, &g, sizeof(g));
         }
     }
@@ -370,6 +375,7 @@ cudaError_t enqueue(const flr_batch_plan *plan, const unsigned char *h_stage,
     a.num_sources = cap;
     a.chan = chan;
     a.partial = partial;
+    a.gb = waveforms ? reinterpret_cast<const flr::GbParams *>(d_stage + lay.gb) : nullptr;
     // the difference forms for XYZ outputs; AET / AE keep the double-float form,
     // whose absolute error stays ~1e-14 of the links: those channels are
     // combinations of X, Y, Z that can cancel to a small fraction of them

@@ -50,6 +50,46 @@ __device__ __forceinline__ f2 from_double(double x) {
 
 __device__ __forceinline__ double to_double(f2 a) { return (double)a.hi + (double)a.lo; }
 
+// x * 2^shift as a df value, from the bits of x with integer operations only
+// (no FP64-pipe conversion; on GB300 that pipe is the scarce one): hi = the
+// top 24 significant bits of x, lo = the next 24 (the remaining 5 dropped),
+// so hi + lo is x to ~2^-48, |lo| < ulp(hi).  Values whose scaled exponent
+// leaves [-100, 100] (zero, tiny, huge, not finite) take the conversion route.
+__device__ __forceinline__ f2 from_double_bits(double x, int shift = 0) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7ffu) - 1023 + shift;
+    if (e < -100 || e > 100) {
+        const double y = ldexp(x, shift);
+        const float hi = __double2float_rn(y);
+        return {hi, __double2float_rn(y - (double)hi)};
+    }
+    const float hi = __uint_as_float(sign | ((unsigned)(e + 127) << 23) |
+                                     (unsigned)((b >> 29) & 0x7fffffu));
+    const unsigned m = (unsigned)(b & 0x1fffffffu);  // the 29 bits below hi
+    if (m == 0u) return {hi, 0.f};
+    const int lz = __clz(m) - 3;                      // leading zeros within the 29 bits
+    const unsigned mant = ((m << (lz + 3)) >> 8) & 0x7fffffu;
+    return {hi, __uint_as_float(sign | ((unsigned)(e - 24 - lz + 127) << 23) | mant)};
+}
+
+// (hi + lo) * 2^shift as a double: both floats widened from their bits (integer
+// operations), one FP64 addition.  Zero and subnormal parts count as zero.
+__device__ __forceinline__ double float_bits_to_double(float v, int shift) {
+    const unsigned u = __float_as_uint(v);
+    const unsigned ef = (u >> 23) & 0xffu;
+    if (ef == 0u) return 0.0;
+    if (ef == 0xffu) return ldexp((double)v, shift);
+    const unsigned long long bits = ((unsigned long long)(u & 0x80000000u) << 32) |
+                                    ((unsigned long long)(ef - 127 + 1023 + shift) << 52) |
+                                    ((unsigned long long)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)bits);
+}
+
+__device__ __forceinline__ double to_double_bits(f2 a, int shift) {
+    return float_bits_to_double(a.hi, shift) + float_bits_to_double(a.lo, shift);
+}
+
 __device__ __forceinline__ f2 renorm(f2 a) { return fast_two_sum(a.hi, a.lo); }
 
 // a + b, result normalised.

@@ -86,6 +86,8 @@ struct FusedTdiSet {
 
 enum FusedChan { kChanXYZ = 0, kChanAET = 1, kChanAE = 2 };
 
+struct GbParams;
+
 struct FusedArgs {
     OrbitTables orb;
     LagrangeTables lt;
@@ -118,6 +120,10 @@ struct FusedArgs {
     int y_halo_hi;             // and after it: TDI delays only look back, so the taps
                                // of a tile's last sample reach h samples past it
     long wait_polls;           // bound of an item's first wait for its staging copy
+    // per-source waveform parameters of a run with waveforms (NULL otherwise):
+    // a source whose h is NULL has its waveform generated into the staged
+    // window instead of read from memory
+    const GbParams *gb;
     int win_max;               // capacity of the staged input window [samples]
     int y_max;                 // capacity of one staged link row [samples]
     double fs;                 // sampling frequency
@@ -140,6 +146,8 @@ struct FusedArgs {
 // Galactic-binary parameters of one source (on-device waveform generation).
 struct GbParams {
     double A, f, fdot, iota, phi0, psi;
+    int model;     // 0: the configurations' binary, 1: the reference tests' GBWave
+    int reserved;
 };
 
 long gb_waveform_chunks(long n);

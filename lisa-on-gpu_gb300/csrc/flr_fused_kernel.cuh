@@ -45,6 +45,7 @@
 #include "flr_df.cuh"
 #include "flr_device.cuh"
 #include "flr_fused.h"
+#include "flr_gbwave.cuh"
 
 namespace flr {
 namespace {
@@ -158,6 +159,83 @@ __device__ __forceinline__ int orbit_segment_fast(const OrbitTables &o, double i
     return (w == o.N - 1) ? o.N - 2 : w;
 }
 
+// Orbit segments of one work item's times, decided from the bits of t (a
+// positive double orders like its bit pattern): the item's times fall in at
+// most three consecutive segments w0 .. w0 + 2; a time farther than 1e-12
+// (relative) from their bounds is in segment w0 + (t >= b1) + (t >= b2),
+// which is the exact (int)(t / dt) (the quotient is then at least 1e-12 w0
+// from an integer, far more than its rounding); other times take the exact
+// lookup.  base[k] = dt * (w0 + k), the product orbit_lerp forms, so lerps
+// from it give the same bits.  The cache saves the FP64 pipe the segment
+// search and that product (GB300's FP64 pipe is the mixed kernel's busiest).
+struct SegCache {
+    long long lo, hi, g1lo, g1hi, g2lo, g2hi;
+    double base[3];
+    int w0;  // -1: not usable (every lookup exact)
+};
+
+struct Seg {
+    int w;        // segment, -1 outside the table
+    double base;  // dt * w
+};
+
+__device__ __forceinline__ void seg_cache_setup(SegCache *c, const OrbitTables &o,
+                                                double inv_dt, double t_lo, double t_hi) {
+    c->w0 = -1;
+    if (!(t_lo > 0.0)) return;
+    const int w0 = orbit_segment_fast(o, inv_dt, t_lo);
+    if (w0 < 1 || w0 + 2 > o.N - 2) return;
+    const double b0 = o.dt * (double)w0, b1 = o.dt * (double)(w0 + 1),
+                 b2 = o.dt * (double)(w0 + 2), b3 = o.dt * (double)(w0 + 3);
+    if (!(t_hi < b3)) return;
+    const double m = 1e-12;
+    c->lo = __double_as_longlong(b0 * (1.0 + m));
+    c->hi = __double_as_longlong(b3 * (1.0 - m));
+    c->g1lo = __double_as_longlong(b1 * (1.0 - m));
+    c->g1hi = __double_as_longlong(b1 * (1.0 + m));
+    c->g2lo = __double_as_longlong(b2 * (1.0 - m));
+    c->g2hi = __double_as_longlong(b2 * (1.0 + m));
+    c->base[0] = b0;
+    c->base[1] = b1;
+    c->base[2] = b2;
+    c->w0 = w0;
+}
+
+__device__ __forceinline__ Seg seg_of(const SegCache *c, const OrbitTables &o, double inv_dt,
+                                      double t) {
+    const long long b = __double_as_longlong(t);
+    const int w0 = c->w0;
+    if (w0 >= 0 && b > c->lo && b < c->hi && (b <= c->g1lo || b >= c->g1hi) &&
+        (b <= c->g2lo || b >= c->g2hi)) {
+        const int k = (int)(b >= c->g1hi) + (int)(b >= c->g2hi);
+        return {w0 + k, c->base[k]};
+    }
+    const int w = orbit_segment_fast(o, inv_dt, t);
+    return {w, (w < 0) ? 0.0 : o.dt * (double)w};
+}
+
+// orbit_lerp with the segment's base time given: m (t - base) + lo
+__device__ __forceinline__ double orbit_lerp_b(const double *tab, const double *slope, int w,
+                                               int stride, int col, double t, double base) {
+    const double lo = __ldg(tab + (size_t)w * stride + col);
+    const double m = __ldg(slope + (size_t)w * stride + col);
+    return m * (t - base) + lo;
+}
+
+__device__ __forceinline__ void position_sb(const OrbitTables &o, Seg g, double t, int sc,
+                                            double out[3]) {
+    const int s = (sc >= 1 && sc <= 3) ? sc - 1 : -1;
+    if (g.w < 0 || s < 0) {
+        out[0] = out[1] = out[2] = 0.0;
+        return;
+    }
+    const double dt_w = t - g.base;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+        out[c] = __ldg(o.x_slope + (size_t)g.w * 9 + 3 * s + c) * dt_w +
+                 __ldg(o.x + (size_t)g.w * 9 + 3 * s + c);
+}
+
 __device__ __forceinline__ void position_seg(const OrbitTables &o, int w, double t, int sc,
                                              double out[3]) {
     int s = (sc >= 1 && sc <= 3) ? sc - 1 : -1;
@@ -252,7 +330,7 @@ __device__ __forceinline__ MixedDelays link_delays_mixed(const OrbitTables &o, d
 // spacecraft receives: its position at t and the receiver delay's split
 // (same operations as there, so the same bits).
 struct ReceiverSide {
-    int w;  // orbit segment of t
+    Seg w;  // orbit segment of t
     int d_rec;
     df::f2 e_rec;
     double x_rec[3];
@@ -260,10 +338,10 @@ struct ReceiverSide {
 
 __device__ __forceinline__ ReceiverSide receiver_mixed(const OrbitTables &o, double inv_dt, int sc,
                                                        double t, double t_first, double fs,
-                                                       const double k[3]) {
+                                                       const double k[3], const SegCache *sc_) {
     ReceiverSide r;
-    r.w = orbit_segment_fast(o, inv_dt, t);
-    position_seg(o, r.w, t, sc, r.x_rec);
+    r.w = seg_of(sc_, o, inv_dt, t);
+    position_sb(o, r.w, t, sc, r.x_rec);
     split_delay_df(t - dot3(k, r.x_rec) * kCInv, t_first, fs, r.d_rec, r.e_rec);
     return r;
 }
@@ -277,12 +355,13 @@ struct EmitterSide {
 };
 
 __device__ __forceinline__ EmitterSide emitter_mixed(const OrbitTables &o, double inv_dt, int slot,
-                                                     int w, double t, double t_first, double fs,
-                                                     const double k[3]) {
+                                                     Seg w, double t, double t_first, double fs,
+                                                     const double k[3], const SegCache *sc_) {
     EmitterSide e;
-    const double L = (w < 0) ? 0.0 : orbit_lerp(o.ltt, o.ltt_slope, w, 6, slot, t, o.dt);
+    const double L =
+        (w.w < 0) ? 0.0 : orbit_lerp_b(o.ltt, o.ltt_slope, w.w, 6, slot, t, w.base);
     const double t_em = t - L;
-    position_seg(o, orbit_segment_fast(o, inv_dt, t_em), t_em, o.sc_e[slot], e.x_em);
+    position_sb(o, seg_of(sc_, o, inv_dt, t_em), t_em, o.sc_e[slot], e.x_em);
     split_delay_df(t_em - dot3(k, e.x_em) * kCInv, t_first, fs, e.d_em, e.e_em);
     return e;
 }
@@ -362,7 +441,7 @@ __device__ __forceinline__ EmitterF64 emitter_f64(const OrbitTables &o, int slot
 // Exact complex interpolation at (d, eps) from the staged raw window when its
 // taps lie in it, else from global memory (the same values); false when the
 // taps leave the input.
-__device__ __forceinline__ bool c128_any(const double2 *hraw, long wlo, int W, const double2 *hg,
+__device__ __forceinline__ bool c128_any(const double2 *hraw, long wlo, int W, const HSrc &hg,
                                          long n, int d, double eps, double A,
                                          const LagrangeTables &lt, double &hp, double &hc) {
     const long lo = (long)d - (lt.h - 1), hi = (long)d + lt.h;
@@ -371,7 +450,7 @@ __device__ __forceinline__ bool c128_any(const double2 *hraw, long wlo, int W, c
         return true;
     }
     if (lo >= 0 && hi < n) {
-        lagrange_c128(GlobalC128{hg}, d, eps, A, lt, hp, hc);
+        lagrange_c128(hg, d, eps, A, lt, hp, hc);
         return true;
     }
     return false;
@@ -403,7 +482,7 @@ __device__ __forceinline__ DfProjection df_projection(const double x_rec[3], con
                                                       const df::f2 v[3]) {
     df::f2 n[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) n[c] = df::from_double(x_rec[c] - x_em[c]);
+    for (int c = 0; c < 3; ++c) n[c] = df::from_double_bits(x_rec[c] - x_em[c]);
     const df::f2 r = df_rsqrt(df_dot3(n, n));
 #pragma unroll
     for (int c = 0; c < 3; ++c) n[c] = df::mul(n[c], r);
@@ -475,15 +554,15 @@ struct DfShared {
 // window falls outside the staged window).
 struct DfGlobal {
     using index_t = long;
-    const double2 *h;
+    HSrc h;
     double scale;
     __device__ __forceinline__ float4 val(long k) const {
-        double2 v = __ldg(h + k);
+        double2 v = h[k];
         df::f2 r = df::from_double(v.x * scale), i = df::from_double(v.y * scale);
         return make_float4(r.hi, r.lo, i.hi, i.lo);
     }
     __device__ __forceinline__ float4 diff(long k) const {
-        double2 a = __ldg(h + k), b = __ldg(h + k + 1);
+        double2 a = h[k], b = h[k + 1];
         df::f2 r = df::from_double((b.x - a.x) * scale), i = df::from_double((b.y - a.y) * scale);
         return make_float4(r.hi, r.lo, i.hi, i.lo);
     }
@@ -537,7 +616,7 @@ __device__ __forceinline__ void df_interp_c128_sbp(const Src &src, typename Src:
 // in it, else from global memory (the same df values); false when the taps
 // leave the input.
 __device__ __forceinline__ bool df_interp_c128_any(const float4 *hdf, const float4 *dh, long wlo,
-                                                   int W, const double2 *hg, double scale, long n,
+                                                   int W, const HSrc &hg, double scale, long n,
                                                    int d, df::f2 A, df::f2 eps, const df::f2 *edf,
                                                    int h, df::f2 &re, df::f2 &im) {
     const long lo = (long)d - (h - 1), hi = (long)d + h;
@@ -874,10 +953,10 @@ struct D3Shared {
 // The same from global memory (taps outside the staged window).
 struct D3Global {
     using index_t = long;
-    const double2 *h;
+    HSrc h;
     double scale;
     __device__ __forceinline__ float4 val(long k) const {
-        const double2 v = __ldg(h + k);
+        const double2 v = h[k];
         const df::f2 r = df::from_double(v.x * scale), i = df::from_double(v.y * scale);
         return make_float4(r.hi, r.lo, i.hi, i.lo);
     }
@@ -940,7 +1019,7 @@ __device__ __forceinline__ void d3_interp_c128(const Src &src, typename Src::ind
 
 // As df_interp_c128_any for the third-difference form.
 __device__ __forceinline__ bool d3_interp_c128_any(const float4 *hdf, const float2 *t3, long wlo,
-                                                   int W, const double2 *hg, double scale, long n,
+                                                   int W, const HSrc &hg, double scale, long n,
                                                    int d, df::f2 e, const D2Weights &w,
                                                    const df::f2 *edf, int h, df::f2 &re,
                                                    df::f2 &im) {
@@ -962,7 +1041,7 @@ __device__ __forceinline__ bool d3_interp_c128_any(const float4 *hdf, const floa
 template <bool kD2>
 __device__ __forceinline__ bool mixed_interp_any(const FusedArgs &a, const float4 *hdf,
                                                  const float4 *dh, long wlo, int W,
-                                                 const double2 *hg, double scale, long n, int d,
+                                                 const HSrc &hg, double scale, long n, int d,
                                                  df::f2 e, df::f2 inv_deps, const df::f2 *edf,
                                                  int h, df::f2 &re, df::f2 &im) {
     if (kD2)
@@ -974,14 +1053,15 @@ __device__ __forceinline__ bool mixed_interp_any(const FusedArgs &a, const float
 
 // -------------------------------------------------------------- the kernel ----
 
-// Register budgets: the grouped mixed instance is sized for three blocks per
-// SM (80 registers), which measured 3 % faster than the compiler's 96
-// registers at two; the others keep the compiler's choice (a minimum of 0
-// blocks leaves it unspecified).
+// Register budgets: the mixed instances are sized for three blocks per SM (80
+// registers; the grouped one measured 3 % faster than at the compiler's 96
+// registers and two blocks, and the plan's persistent grid is sized for the
+// instances together); the FP64 and the diagnostics instances keep the
+// compiler's choice (a minimum of 0 blocks leaves it unspecified).
 // kInner: the instance that forms per-tile inner products with FusedSource
 // data (FusedArgs::partial) and writes the channels only where out is set.
 template <bool kMixed, bool kDiag, bool kGrouped, bool kInner, bool kD2>
-__global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 0)
+__global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
     fused_kernel(const FusedArgs a) {
     static_assert(kMixed || !kD2, "the difference forms are mixed-arithmetic forms");
     static_assert(kMixed || !kGrouped, "the grouped form is a mixed-arithmetic form");
@@ -990,7 +1070,9 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
     const Layout lay = layout(kMixed, a.win_max, a.y_max);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     double *scale_sm = reinterpret_cast<double *>(smem + 16);
+    int *scale_exp_sm = reinterpret_cast<int *>(smem + 24);  // scale = 2^(*scale_exp_sm)
     int *win_sm = reinterpret_cast<int *>(smem + 32);  // [0] = min d, [1] = max d
+    SegCache *segc = reinterpret_cast<SegCache *>(smem + 128);  // the item's orbit segments
     double *warp_max = reinterpret_cast<double *>(smem + 64);
     FusedTdiSet *set = reinterpret_cast<FusedTdiSet *>(smem + lay.set);
     df::f2 *edf = reinterpret_cast<df::f2 *>(smem + lay.edf);
@@ -1025,6 +1107,9 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
         }
         const long tile_idx = wi - __ldg(a.tile_base + si);
         const FusedSource &src = a.sources[si];
+        // the input outside the staged window: the stored waveform, or the
+        // source's generator when it has none
+        const HSrc hsrc{src.h, a.gb ? a.gb + si : nullptr, src.t0, a.dt};
         const long n = src.n;
         const int ps = src.ps, ts = src.ts;
         const double t0 = src.t0;
@@ -1070,6 +1155,11 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
         if (tid == 0) {
             win_sm[0] = 0x7fffffff;
             win_sm[1] = -0x7fffffff;
+            // the item's times: its link-stream samples, and their emission
+            // times up to 100 s earlier
+            if (kMixed)
+                seg_cache_setup(segc, a.orb, a.inv_orbit_dt, t0 + (double)ya * a.dt - 100.0,
+                                t0 + (double)yb * a.dt);
         }
         __syncthreads();
         if (tid < 12 && yfirst < ylast) {
@@ -1098,8 +1188,14 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
             W = (int)max(0L, min(whi - wlo, (long)a.win_max));
         }
 
-        // 2. stage the window with one bulk copy
-        if (W > 0) {
+        // 2. stage the window: generated in place for a source without a stored
+        // waveform, else one bulk copy
+        if (W > 0 && src.h == nullptr) {
+            const GbCoefs gc = gb_coefs(a.gb[si]);
+            for (int i = tid; i < W; i += kThreads)
+                hraw[i] = gb_sample(gc, t0 + (double)(wlo + i) * a.dt);
+            __syncthreads();
+        } else if (W > 0) {
             if (tid == 0) {
                 fence_proxy_async();
                 mbar_expect_tx(bar, (uint32_t)W * 16u);
@@ -1131,8 +1227,10 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
             phase ^= 1u;
         }
 
-        // 3. mixed: scale to ~1 by a power of two, split into df, first differences
+        // 3. mixed: scale to ~1 by a power of two, split into df (from the bits:
+        // the power of two goes into the exponent), first differences
         double scale = 1.0;
+        int sexp = 0;
         if (kMixed) {
             double m = 0.0;
             for (int i = tid; i < W; i += kThreads) {
@@ -1147,18 +1245,16 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
                 double mm = 0.0;
                 for (int i = 0; i < kThreads / 32; ++i) mm = fmax(mm, warp_max[i]);
                 int ex = 0;
-                double s = 1.0;
-                if (mm > 0.0 && mm < 1e300) {
-                    frexp(mm, &ex);
-                    s = ldexp(1.0, -ex);
-                }
-                *scale_sm = s;
+                if (mm > 0.0 && mm < 1e300) frexp(mm, &ex);
+                *scale_sm = ldexp(1.0, -ex);
+                *scale_exp_sm = -ex;
             }
             __syncthreads();
             scale = *scale_sm;
+            sexp = *scale_exp_sm;
             for (int i = tid; i < W; i += kThreads) {
                 const double2 q = hraw[i];
-                df::f2 r = df::from_double(q.x * scale), im = df::from_double(q.y * scale);
+                const df::f2 r = df::from_double_bits(q.x, sexp), im = df::from_double_bits(q.y, sexp);
                 hdf[i] = make_float4(r.hi, r.lo, im.hi, im.lo);
                 if (!kD2 && i + 1 < W) {
                     const double2 q1 = hraw[i + 1];
@@ -1204,11 +1300,12 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
                 df::f2 re_r = {0.f, 0.f}, im_r = {0.f, 0.f}, re_e = {0.f, 0.f}, im_e = {0.f, 0.f};
                 bool ok_r = false, ok_e = false;
                 if (live) {
-                    rs = receiver_mixed(a.orb, a.inv_orbit_dt, rr + 1, t, t0, a.fs, k);
-                    ok_r = mixed_interp_any<kD2>(a, hdf, dh, wlo, W, src.h, scale, n, rs.d_rec,
+                    rs = receiver_mixed(a.orb, a.inv_orbit_dt, rr + 1, t, t0, a.fs, k, segc);
+                    ok_r = mixed_interp_any<kD2>(a, hdf, dh, wlo, W, hsrc, scale, n, rs.d_rec,
                                             rs.e_rec, inv_deps_df, edf, h, re_r, im_r);
-                    es = emitter_mixed(a.orb, a.inv_orbit_dt, a.tx_slot[rr], rs.w, t, t0, a.fs, k);
-                    ok_e = mixed_interp_any<kD2>(a, hdf, dh, wlo, W, src.h, scale, n, es.d_em,
+                    es = emitter_mixed(a.orb, a.inv_orbit_dt, a.tx_slot[rr], rs.w, t, t0, a.fs, k,
+                                       segc);
+                    ok_e = mixed_interp_any<kD2>(a, hdf, dh, wlo, W, hsrc, scale, n, es.d_em,
                                             es.e_em, inv_deps_df, edf, h, re_e, im_e);
                 }
                 const bool own = live && (j >= o0 && j < o1);  // diagnostics
@@ -1261,20 +1358,20 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
                 const double t = t0 + (double)j * a.dt;
                 const bool own = (j >= o0 && j < o1);  // this tile's outputs: diagnostics
                 const ReceiverSide rs =
-                    receiver_mixed(a.orb, a.inv_orbit_dt, a.rx_sc[r], t, t0, a.fs, k);
+                    receiver_mixed(a.orb, a.inv_orbit_dt, a.rx_sc[r], t, t0, a.fs, k, segc);
                 df::f2 re_r, im_r;
-                const bool ok_r = mixed_interp_any<kD2>(a, hdf, dh, wlo, W, src.h, scale, n, rs.d_rec,
+                const bool ok_r = mixed_interp_any<kD2>(a, hdf, dh, wlo, W, hsrc, scale, n, rs.d_rec,
                                                    rs.e_rec, inv_deps_df, edf, h, re_r, im_r);
                 for (int q = 0; q < 2; ++q) {
                     const int slot = a.rx_slot[r][q];
                     const EmitterSide es =
-                        emitter_mixed(a.orb, a.inv_orbit_dt, slot, rs.w, t, t0, a.fs, k);
+                        emitter_mixed(a.orb, a.inv_orbit_dt, slot, rs.w, t, t0, a.fs, k, segc);
                     if (kDiag && own && src.d_rec_out) {
                         src.d_rec_out[(long)slot * n + j] = rs.d_rec;
                         src.d_em_out[(long)slot * n + j] = es.d_em;
                     }
                     df::f2 re_e, im_e;
-                    const bool ok_e = mixed_interp_any<kD2>(a, hdf, dh, wlo, W, src.h, scale, n,
+                    const bool ok_e = mixed_interp_any<kD2>(a, hdf, dh, wlo, W, hsrc, scale, n,
                                                        es.d_em, es.e_em, inv_deps_df, edf, h,
                                                        re_e, im_e);
                     if (!ok_r || !ok_e) {
@@ -1315,13 +1412,13 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
                     rs = receiver_f64(a.orb, rr + 1, t, t0, a.fs, k);
                     double A_r;
                     okA_r = prefactor(a.lt, rs.e_rec, A_r);
-                    okT_r = okA_r && c128_any(hraw, wlo, W, src.h, n, rs.d_rec, rs.e_rec, A_r,
+                    okT_r = okA_r && c128_any(hraw, wlo, W, hsrc, n, rs.d_rec, rs.e_rec, A_r,
                                               a.lt, hp_r, hc_r);
                     double e_em, A_e;
                     emitter_side_f64(a.orb, rr + 1, t, light_travel_time(a.orb, t, a.tx_slot[rr]),
                                      t0, a.fs, k, x_em, d_em, e_em);
                     okA_e = prefactor(a.lt, e_em, A_e);
-                    okT_e = okA_e && c128_any(hraw, wlo, W, src.h, n, d_em, e_em, A_e, a.lt,
+                    okT_e = okA_e && c128_any(hraw, wlo, W, hsrc, n, d_em, e_em, A_e, a.lt,
                                               hp_e, hc_e);
                 }
                 const bool own = live && (j >= o0 && j < o1);  // diagnostics
@@ -1381,7 +1478,7 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
                 const ReceiverF64 rs = receiver_f64(a.orb, a.rx_sc[r], t, t0, a.fs, k);
                 double A_r, hp_r = 0.0, hc_r = 0.0;
                 const bool okA_r = prefactor(a.lt, rs.e_rec, A_r);
-                const bool okT_r = okA_r && c128_any(hraw, wlo, W, src.h, n, rs.d_rec, rs.e_rec,
+                const bool okT_r = okA_r && c128_any(hraw, wlo, W, hsrc, n, rs.d_rec, rs.e_rec,
                                                      A_r, a.lt, hp_r, hc_r);
                 for (int q = 0; q < 2; ++q) {
                     const int slot = a.rx_slot[r][q];
@@ -1397,7 +1494,7 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
                         out = qnan();
                     } else {
                         double hp_e, hc_e;
-                        const bool okT_e = c128_any(hraw, wlo, W, src.h, n, es.d_em, es.e_em,
+                        const bool okT_e = c128_any(hraw, wlo, W, hsrc, n, es.d_em, es.e_em,
                                                     A_e, a.lt, hp_e, hc_e);
                         if (okT_r && okT_e) {
                             double pre = 1. / (1. - es.k_dot_n);
@@ -1442,9 +1539,9 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
                         y32[slot * a.y_max + jj] = make_float2(__int_as_float(0x7fc00000), 0.f);
                         continue;
                     }
-                    mixed_interp_any<kD2>(a, hdf, dh, wlo, W, src.h, scale, n, g.d_rec, e_r,
+                    mixed_interp_any<kD2>(a, hdf, dh, wlo, W, hsrc, scale, n, g.d_rec, e_r,
                                      inv_deps_df, edf, h, re_r, im_r);
-                    mixed_interp_any<kD2>(a, hdf, dh, wlo, W, src.h, scale, n, g.d_em, e_e,
+                    mixed_interp_any<kD2>(a, hdf, dh, wlo, W, hsrc, scale, n, g.d_em, e_e,
                                      inv_deps_df, edf, h, re_e, im_e);
                 } else if (lo >= wlo && hi + 1 < wlo + W) {
                     const df::f2 A_r = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_r);
@@ -1455,7 +1552,7 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
                 } else if (lo >= 0 && hi + 1 < n) {
                     const df::f2 A_r = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_r);
                     const df::f2 A_e = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_e);
-                    const DfGlobal s{src.h, scale};
+                    const DfGlobal s{hsrc, scale};
                     df_interp_c128_sbp(s, g.d_rec, A_r, e_r, edf, h, re_r, im_r);
                     df_interp_c128_sbp(s, g.d_em, A_e, e_e, edf, h, re_e, im_e);
                 } else {
@@ -1492,7 +1589,7 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
                         lagrange_c128(s, (int)(g.d_rec - wlo), g.e_rec, A_r, a.lt, hp_r, hc_r);
                         lagrange_c128(s, (int)(g.d_em - wlo), g.e_em, A_e, a.lt, hp_e, hc_e);
                     } else {
-                        const GlobalC128 s{src.h};
+                        const HSrc &s = hsrc;
                         lagrange_c128(s, g.d_rec, g.e_rec, A_r, a.lt, hp_r, hc_r);
                         lagrange_c128(s, g.d_em, g.e_em, A_e, a.lt, hp_e, hc_e);
                     }
@@ -1537,15 +1634,15 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
         }
 
         // 5. TDI for the output samples [o0, o1)
-        const double inv_scale = 1.0 / scale;
         double lk[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // inner products (kInner)
         if (kGrouped) {
             for (long i = o0 + tid; i < o1; i += kThreads) {
                 const double t = t0 + (double)i * a.dt;
-                const int w = orbit_segment_fast(a.orb, a.inv_orbit_dt, t);
+                const Seg w = seg_of(segc, a.orb, a.inv_orbit_dt, t);
                 // every link has this L(t): the delay of a list of length m is t - L - ... - L
                 const double L0 =
-                    (w < 0) ? 0.0 : orbit_lerp(a.orb.ltt, a.orb.ltt_slope, w, 6, 0, t, a.orb.dt);
+                    (w.w < 0) ? 0.0
+                              : orbit_lerp_b(a.orb.ltt, a.orb.ltt_slope, w.w, 6, 0, t, w.base);
                 df::f2 accdf[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
                 double delay = t;
                 int depth = 0;
@@ -1586,9 +1683,9 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
 #pragma unroll
                     for (int c = 0; c < 3; ++c) accdf[c] = df::add(accdf[c], val[c]);
                 }
-                const double X = df::to_double(accdf[0]) * inv_scale;
-                const double Yc = df::to_double(accdf[1]) * inv_scale;
-                const double Z = df::to_double(accdf[2]) * inv_scale;
+                const double X = df::to_double_bits(accdf[0], -sexp);
+                const double Yc = df::to_double_bits(accdf[1], -sexp);
+                const double Z = df::to_double_bits(accdf[2], -sexp);
                 if (!kInner || src.out) store_channels(src.out, n, i, a.chan, X, Yc, Z);
                 if (kInner && src.data) add_inner(lk, src.data, n, i, a.chan, X, Yc, Z);
             }
@@ -1597,11 +1694,13 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
                 const double t = t0 + (double)i * a.dt;
                 double L[kLinks];
                 if (kMixed) {
-                    const int w = orbit_segment_fast(a.orb, a.inv_orbit_dt, t);
+                    const Seg w = seg_of(segc, a.orb, a.inv_orbit_dt, t);
+                    const double dt_w = t - w.base;
 #pragma unroll
                     for (int s = 0; s < kLinks; ++s)
-                        L[s] = (w < 0) ? 0.0 : orbit_lerp(a.orb.ltt, a.orb.ltt_slope, w, 6, s, t,
-                                                          a.orb.dt);
+                        L[s] = (w.w < 0) ? 0.0
+                                         : __ldg(a.orb.ltt_slope + (size_t)w.w * 6 + s) * dt_w +
+                                               __ldg(a.orb.ltt + (size_t)w.w * 6 + s);
                 } else {
 #pragma unroll
                     for (int s = 0; s < kLinks; ++s) L[s] = light_travel_time(a.orb, t, s);
@@ -1674,9 +1773,9 @@ __global__ void __launch_bounds__(kThreads, ((kGrouped || kD2) && !kDiag) ? 3 : 
                 }
                 double X, Yc, Z;
                 if (kMixed) {
-                    X = df::to_double(accdf[0]) * inv_scale;
-                    Yc = df::to_double(accdf[1]) * inv_scale;
-                    Z = df::to_double(accdf[2]) * inv_scale;
+                    X = df::to_double_bits(accdf[0], -sexp);
+                    Yc = df::to_double_bits(accdf[1], -sexp);
+                    Z = df::to_double_bits(accdf[2], -sexp);
                 } else {
                     X = acc64[0];
                     Yc = acc64[1];

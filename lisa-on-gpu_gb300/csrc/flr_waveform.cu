@@ -1,13 +1,7 @@
-// On-device galactic-binary waveforms for batches of sources.
-//
-// h(t) = hp + i hc with
-//   Phi = phi0 + 2 pi (f t + fdot t^2 / 2),
-//   hp0 = A (1 + cos^2 iota) cos Phi,   hc0 = -2 A cos iota sin Phi,
-//   hp  = hp0 cos 2psi - hc0 sin 2psi,  hc  = hp0 sin 2psi + hc0 cos 2psi,
-// at t_i = t0 + i dt, the drifting-monochromatic binary of the benchmark
-// configurations.  Evaluated in FP64 in the operation order of the host
-// generator (fastlisaresponse_gb300.waveforms.gb_waveform) with CUDA's double
-// sincos, so it agrees with the host generator to a few ulp.
+// On-device galactic-binary waveforms for batches of sources, written to
+// memory (sources with a waveform buffer; the others are generated by the
+// fused kernel while it stages its input).  The models are those of
+// flr_gbwave.cuh, at t_i = t0 + i dt.
 //
 // One persistent launch covers every source of a batch: work items are
 // (source, chunk of kChunk samples), strided over the grid; the source of a
@@ -15,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include "flr_fused.h"
+#include "flr_gbwave.cuh"
 
 namespace flr {
 namespace {
@@ -37,23 +32,12 @@ gb_waveform_kernel(const FusedSource *src, const GbParams *par, const long *chun
                 hi = mid - 1;
         }
         const FusedSource &s = src[lo];
-        const GbParams p = par[lo];
+        if (s.h == nullptr) continue;  // generated inside the fused kernel instead
+        const GbCoefs g = gb_coefs(par[lo]);
         const long i0 = (c - chunk_start[lo]) * kChunk;
-        const double cosi = cos(p.iota);
-        const double amp_p = p.A * (1.0 + cosi * cosi);
-        const double amp_c = -2.0 * p.A * cosi;
-        double s2, c2;
-        sincos(2.0 * p.psi, &s2, &c2);
         double2 *h = const_cast<double2 *>(s.h);
-        for (long i = i0 + threadIdx.x; i < min(i0 + kChunk, s.n); i += kThreads) {
-            const double t = s.t0 + (double)i * dt;
-            const double phase = p.phi0 + 6.283185307179586 * (p.f * t + 0.5 * p.fdot * t * t);
-            double sp, cp;
-            sincos(phase, &sp, &cp);
-            const double hp0 = amp_p * cp;
-            const double hc0 = amp_c * sp;
-            h[i] = make_double2(hp0 * c2 - hc0 * s2, hp0 * s2 + hc0 * c2);
-        }
+        for (long i = i0 + threadIdx.x; i < min(i0 + kChunk, s.n); i += kThreads)
+            h[i] = gb_sample(g, s.t0 + (double)i * dt);
     }
 }
 

@@ -55,7 +55,12 @@ class _TdiUnits(ctypes.Structure):
 
 class _GbParams(ctypes.Structure):
     _fields_ = [("A", ctypes.c_double), ("f", ctypes.c_double), ("fdot", ctypes.c_double),
-                ("iota", ctypes.c_double), ("phi0", ctypes.c_double), ("psi", ctypes.c_double)]
+                ("iota", ctypes.c_double), ("phi0", ctypes.c_double), ("psi", ctypes.c_double),
+                ("model", ctypes.c_int), ("reserved", ctypes.c_int)]
+
+
+# waveform models of the device generator (include/flr_gb300.h)
+GB_MODELS = {"config": 0, "gbwave": 1}
 
 
 class _Source(ctypes.Structure):
@@ -122,6 +127,20 @@ SOURCE_DTYPE = np.dtype(_Source)
 GB_DTYPE = np.dtype(_GbParams)
 GRAPH_WAVEFORMS = 0x1
 GRAPH_DIAGNOSTICS = 0x2
+
+
+def _waveform_buffers(h, lengths, device, keep_waveforms):
+    """Waveform buffers of a run with generated waveforms: the caller's, new
+    ones, or (keep_waveforms False) None for each source: generated inside
+    the fused kernel."""
+    if not keep_waveforms:
+        return [None] * len(lengths)
+    hs = list(h) if h is not None else [
+        torch.empty(n, dtype=torch.complex128, device=device) for n in lengths]
+    for i, n in enumerate(lengths):
+        if hs[i].numel() != n or hs[i].dtype != torch.complex128 or not hs[i].is_cuda:
+            raise ValueError(f"h[{i}] must be a complex128 CUDA buffer of {n} samples")
+    return hs
 
 
 class BatchedResponseTDI:
@@ -276,7 +295,8 @@ class BatchedResponseTDI:
                          self._bucket(len(hs), False, diagnostics) if use_graph else None)
 
     def run_gb(self, params, lengths, lam, beta, t0=0.0, tdi_set=0, h=None, out=None,
-               stream=None, use_graph: bool = False):
+               stream=None, use_graph: bool = False, model: str = "config",
+               keep_waveforms: bool = True):
         """Generate galactic-binary waveforms on the device and evaluate them.
 
         Args:
@@ -287,21 +307,23 @@ class BatchedResponseTDI:
                 that receive the waveforms (allocated when omitted).
             out: optional list of (3, n) float64 CUDA tensors.
             use_graph: as for __call__.
+            model: "config" (the configurations' binary, waveforms.gb_waveform)
+                or "gbwave" (the reference test-suite's generator,
+                waveforms.GBWave).
+            keep_waveforms: False generates each waveform inside the fused
+                kernel, straight into its staged input window, so the
+                waveforms never reach memory (24 B of HBM per output sample:
+                the channels); ``h`` is then ignored and None returned for it.
         Returns:
             (outs, hs): the TDI channels and the generated waveforms.
         """
         params = np.asarray(params, dtype=np.float64).reshape(-1, 6)
         ns = len(params)
         lengths = [int(n) for n in np.broadcast_to(np.asarray(lengths, dtype=np.int64), (ns,))]
-        dev = self.device
-        hs = list(h) if h is not None else [
-            torch.empty(n, dtype=torch.complex128, device=dev) for n in lengths]
-        for i, n in enumerate(lengths):
-            if hs[i].numel() != n or hs[i].dtype != torch.complex128 or not hs[i].is_cuda:
-                raise ValueError(f"h[{i}] must be a complex128 CUDA buffer of {n} samples")
+        hs = _waveform_buffers(h, lengths, self.device, keep_waveforms)
         outs = self._run(hs, params, lengths, lam, beta, t0, tdi_set, out, stream, False,
-                         self._bucket(ns, True, False) if use_graph else None)
-        return outs, hs
+                         self._bucket(ns, True, False) if use_graph else None, model=model)
+        return outs, (hs if keep_waveforms else None)
 
     def inner_products(self, h: Sequence, lam, beta, data: Sequence, t0=0.0, tdi_set=0,
                        stream=None, write_out: bool = False):
@@ -331,24 +353,21 @@ class BatchedResponseTDI:
         return (inner, outs) if write_out else inner
 
     def inner_products_gb(self, params, lengths, lam, beta, data: Sequence, t0=0.0, tdi_set=0,
-                          h=None, stream=None):
+                          h=None, stream=None, model: str = "config",
+                          keep_waveforms: bool = True):
         """inner_products() of galactic binaries whose waveforms are generated
-        on the device (run_gb's parameters); the channels are not stored.
-        Returns ((ns, 2, 3) inner products, waveforms)."""
+        on the device (run_gb's parameters, model and keep_waveforms); the
+        channels are not stored.  Returns ((ns, 2, 3) inner products,
+        waveforms or None)."""
         params = np.asarray(params, dtype=np.float64).reshape(-1, 6)
         ns = len(params)
         lengths = [int(n) for n in np.broadcast_to(np.asarray(lengths, dtype=np.int64), (ns,))]
-        dev = self.device
-        hs = list(h) if h is not None else [
-            torch.empty(n, dtype=torch.complex128, device=dev) for n in lengths]
-        for i, n in enumerate(lengths):
-            if hs[i].numel() != n or hs[i].dtype != torch.complex128 or not hs[i].is_cuda:
-                raise ValueError(f"h[{i}] must be a complex128 CUDA buffer of {n} samples")
+        hs = _waveform_buffers(h, lengths, self.device, keep_waveforms)
         ds = self._check_data(data, lengths)
-        inner = torch.empty((ns, 6), dtype=torch.float64, device=dev)
+        inner = torch.empty((ns, 6), dtype=torch.float64, device=self.device)
         self._run(hs, params, lengths, lam, beta, t0, tdi_set, None, stream, False, None,
-                  data=ds, inner=inner, write_out=False)
-        return inner.view(ns, 2, 3), hs
+                  data=ds, inner=inner, write_out=False, model=model)
+        return inner.view(ns, 2, 3), (hs if keep_waveforms else None)
 
     def run_host(self, h: Sequence, lam, beta, t0=0.0, tdi_set=0, out: Optional[Sequence] = None,
                  chunks: int = 4, group_samples: Optional[int] = None):
@@ -583,7 +602,7 @@ class BatchedResponseTDI:
 
     # -- internals ----------------------------------------------------------------
     def _run(self, hs, params, lengths, lam, beta, t0, tdi_set, out, stream, diagnostics, graph,
-             data=None, inner=None, write_out=True, out_range=None):
+             data=None, inner=None, write_out=True, out_range=None, model="config"):
         ns = len(hs)
         dev = self.device
         lam = np.broadcast_to(np.asarray(lam, dtype=np.float64), (ns,))
@@ -604,7 +623,7 @@ class BatchedResponseTDI:
         else:
             outs = None
         srcs = np.zeros(ns, dtype=SOURCE_DTYPE)
-        srcs["h"] = [x.data_ptr() for x in hs]
+        srcs["h"] = [0 if x is None else x.data_ptr() for x in hs]
         if outs is not None:
             srcs["out"] = [o.data_ptr() for o in outs]
         if out_range is not None:
@@ -634,7 +653,13 @@ class BatchedResponseTDI:
                 srcs["d_tdi_out"][i] = dg["d_tdi"].data_ptr()
         gbs = None
         if params is not None:
-            gbs = np.ascontiguousarray(params, dtype=np.float64).view(GB_DTYPE).reshape(ns)
+            prm = np.ascontiguousarray(params, dtype=np.float64).reshape(ns, 6)
+            gbs = np.zeros(ns, dtype=GB_DTYPE)
+            for k, name in enumerate(("A", "f", "fdot", "iota", "phi0", "psi")):
+                gbs[name] = prm[:, k]
+            if model not in GB_MODELS:
+                raise ValueError(f"model must be one of {sorted(GB_MODELS)}")
+            gbs["model"] = GB_MODELS[model]
         if stream is None:
             stream = torch.cuda.current_stream(dev)
         lib = _plan_fns()
@@ -715,7 +740,7 @@ class BatchGraph:
                       diagnostics, self)
 
     def run_gb(self, params, lengths, lam, beta, t0=0.0, tdi_set=0, h=None, out=None,
-               stream=None):
+               stream=None, model: str = "config", keep_waveforms: bool = True):
         if not self.waveforms:
             raise ValueError("this graph was created without waveforms")
         o = self.owner
@@ -723,12 +748,10 @@ class BatchGraph:
         ns = len(params)
         self._check(ns)
         lengths = [int(n) for n in np.broadcast_to(np.asarray(lengths, dtype=np.int64), (ns,))]
-        hs = list(h) if h is not None else [
-            torch.empty(n, dtype=torch.complex128, device=o.device) for n in lengths]
-        for i, n in enumerate(lengths):
-            if hs[i].numel() != n or hs[i].dtype != torch.complex128 or not hs[i].is_cuda:
-                raise ValueError(f"h[{i}] must be a complex128 CUDA buffer of {n} samples")
-        return o._run(hs, params, lengths, lam, beta, t0, tdi_set, out, stream, False, self), hs
+        hs = _waveform_buffers(h, lengths, o.device, keep_waveforms)
+        outs = o._run(hs, params, lengths, lam, beta, t0, tdi_set, out, stream, False, self,
+                      model=model)
+        return outs, (hs if keep_waveforms else None)
 
     def _check(self, ns):
         if ns > self.max_sources:

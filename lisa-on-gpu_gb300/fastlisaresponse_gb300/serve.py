@@ -3,12 +3,13 @@
 Many likelihood samplers submit single evaluations -- a galactic-binary
 source (7 waveform/sky parameters), a length and a TDI generation -- at any
 time.  :class:`ResponseServer` keeps the orbit and Lagrange tables resident on
-the GPU, admits requests against an HBM budget (each request needs its
-waveform and its three output channels, 40 bytes per sample), and packs the
-admitted requests into one launch pair per batch: an on-device waveform
-kernel followed by the persistent fused response + TDI kernel
-(:meth:`BatchedResponseTDI.run_gb`), replayed from the CUDA graph of the
-batch's size bucket (sources rounded up to a power of two; lengths are free).
+the GPU, admits requests against an HBM budget (each request needs its three
+output channels, 24 bytes per sample: its waveform is generated inside the
+kernel, straight into the staged input window), and packs the admitted
+requests into one persistent fused response + TDI launch per batch
+(:meth:`BatchedResponseTDI.run_gb` with ``keep_waveforms=False``), replayed
+from the CUDA graph of the batch's size bucket (sources rounded up to a power
+of two; lengths are free).
 Batches go to ``num_streams`` CUDA
 streams, so a batch formed from requests that arrived while others were
 running starts right away and overlaps with them on the device; memory
@@ -36,7 +37,7 @@ from typing import List, Optional, Sequence
 
 import numpy as np
 
-BYTES_PER_SAMPLE = 16 + 24  # complex128 waveform + three float64 channels
+BYTES_PER_SAMPLE = 24  # three float64 channels (waveforms are generated in the kernel)
 
 
 @dataclass
@@ -123,13 +124,15 @@ class GpuExecutor:
         with torch.cuda.device(self.device), torch.cuda.stream(s):
             outs = [torch.empty((3, r.n), dtype=torch.float64, device=self.device)
                     for r in batch]
-            hs = [torch.empty(r.n, dtype=torch.complex128, device=self.device) for r in batch]
+            # waveforms generated inside the fused kernel: only the channels
+            # reach memory
             self.plans[lane].run_gb(params, [r.n for r in batch], lam, beta,
                                     t0=[r.t0 for r in batch], tdi_set=[r.tdi_set for r in batch],
-                                    h=hs, out=outs, stream=s, use_graph=self.use_graphs)
+                                    out=outs, stream=s, use_graph=self.use_graphs,
+                                    keep_waveforms=False)
             ev = torch.cuda.Event()
             ev.record(s)
-        return (ev, outs, hs)
+        return (ev, outs)
 
     def finished(self, handle) -> bool:
         return handle[0].query()

@@ -55,6 +55,8 @@ def test_same_result_alone_and_in_the_mix(gpu_lib):
 
 
 def test_device_waveform_matches_host_generator(gpu_lib):
+    """Both device models against their host generators: the configurations'
+    binary (waveforms.gb_waveform) and the reference tests' GBWave."""
     import fastlisaresponse_gb300 as flr
 
     dt = 10.0
@@ -68,3 +70,39 @@ def test_device_waveform_matches_host_generator(gpu_lib):
         host = flr.gb_waveform(*prm[i], t0[i] + np.arange(n[i]) * dt)
         dev = hs[i].cpu().numpy()
         assert np.max(np.abs(dev - host)) <= 1e-12 * np.max(np.abs(host))
+    # the reference tests' generator (t from 0, as GBWave's arange)
+    _, hs = bat.run_gb(prm, n, [1.0, 2.0], [0.3, -0.4], model="gbwave")
+    for i in range(2):
+        host = flr.GBWave()(*prm[i], T=n[i] * dt / flr.waveforms.YRSID_SI, dt=dt)[:n[i]]
+        dev = hs[i].cpu().numpy()
+        assert np.max(np.abs(dev - host)) <= 1e-12 * np.max(np.abs(host))
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("model", ["config", "gbwave"])
+def test_waveforms_generated_in_the_kernel(gpu_lib, precision, model):
+    """keep_waveforms=False generates each waveform straight into the fused
+    kernel's staged window (nothing written to memory): the same bits as the
+    run that stores the waveforms first, directly and through a graph."""
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+
+    dt = 10.0
+    orb = flr.EqualArmlengthOrbits(t_max=1.3e6)
+    bat = flr.BatchedResponseTDI(1 / dt, tdi="2nd generation", orbits=orb, precision=precision)
+    rng = np.random.default_rng(9)
+    p = flr.waveforms.draw_gb_parameters(rng, 5)
+    prm = np.stack([p[k] for k in ("A", "f", "fdot", "iota", "phi0", "psi")], axis=1)
+    n = [4000, 31000, 2**16 + 7, 9000, 100001]
+    t0 = [0.0, 1000.0, 0.0, 2.5e4, 0.0]
+    kw = dict(t0=t0, tdi_set=0, model=model)
+    want, hs = bat.run_gb(prm, n, p["lam"], p["beta"], **kw)
+    got, none = bat.run_gb(prm, n, p["lam"], p["beta"], keep_waveforms=False, **kw)
+    assert none is None
+    for a, b in zip(got, want):
+        assert torch.equal(a, b)
+    got, _ = bat.run_gb(prm, n, p["lam"], p["beta"], keep_waveforms=False, use_graph=True, **kw)
+    for a, b in zip(got, want):
+        assert torch.equal(a, b)
+    assert bat.status() == 0
