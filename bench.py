@@ -916,31 +916,46 @@ def run_reference(args):
 
 
 def run_profile_batch(spec: str) -> None:
-    """Small batched case for ncu captures: 16 galactic binaries x 2^18
-    samples at dt = 10 s, 2nd-gen TDI, order 25; spec = "<fp64|mixed>:<equal|kepler>".
-    Two calls of the batch (the capture takes the first)."""
+    """Small batched cases for ncu captures, spec = "<fp64|mixed>:<kind>":
+    kind equal|kepler: 16 galactic binaries x 2^18 samples at dt = 10 s with
+    equal-arm or Keplerian orbits; kind batch64: the first 64 sources of the
+    batching configuration (49.3 M samples, 2.0 GB of inputs and outputs).
+    2nd-gen TDI XYZ, order 25.  Two calls of the batch (the capture takes the
+    first)."""
     import torch
 
     import fastlisaresponse_gb300 as flr
 
     prec, kind = spec.split(":")
     dev = torch.device("cuda", 0)
-    dt, ns, n = 10.0, 16, 2**18
-    rng = np.random.default_rng(5)
-    t_max = orbit_t_max(n, dt)
-    orb = flr.EqualArmlengthOrbits(t_max=t_max) if kind == "equal" else \
-        flr.KeplerianOrbits(t_max=t_max)
-    p = flr.waveforms.draw_gb_parameters(rng, ns)
-    t = torch.arange(n, dtype=torch.float64, device=dev) * dt
-    hs = [flr.gb_waveform(p["A"][i], p["f"][i], p["fdot"][i], p["iota"][i], p["phi0"][i],
-                          p["psi"][i], t) for i in range(ns)]
+    dt = 10.0
+    if kind == "batch64":
+        lengths, p = batch_sources(BATCH["sources"])
+        idx = list(range(64))
+        lengths = lengths[:64]
+        hs = _device_waveforms(lengths, p, idx, dt, dev)
+        lam, beta = p["lam"][idx], p["beta"][idx]
+        orb = flr.EqualArmlengthOrbits(t_max=orbit_t_max(int(lengths.max()), dt))
+    else:
+        ns, n = 16, 2**18
+        rng = np.random.default_rng(5)
+        t_max = orbit_t_max(n, dt)
+        orb = flr.EqualArmlengthOrbits(t_max=t_max) if kind == "equal" else \
+            flr.KeplerianOrbits(t_max=t_max)
+        p = flr.waveforms.draw_gb_parameters(rng, ns)
+        t = torch.arange(n, dtype=torch.float64, device=dev) * dt
+        hs = [flr.gb_waveform(p["A"][i], p["f"][i], p["fdot"][i], p["iota"][i], p["phi0"][i],
+                              p["psi"][i], t) for i in range(ns)]
+        lam, beta = p["lam"], p["beta"]
     bat = flr.BatchedResponseTDI(1 / dt, order=25, tdi="2nd generation", orbits=orb,
                                  precision=prec)
     for _ in range(2):
-        bat(hs, p["lam"], p["beta"])
+        bat(hs, lam, beta)
     torch.cuda.synchronize()
     assert bat.status() == 0
-    print(json.dumps({"profile_batch": spec, "plan": bat.plan_info}))
+    samples = sum(len(h) - 2 * bat.tdi_start_ind for h in hs)
+    print(json.dumps({"profile_batch": spec, "computed_samples": samples,
+                      "plan": bat.plan_info}))
 
 
 def main():
@@ -959,7 +974,7 @@ def main():
     ap.add_argument("--details", default=None, metavar="FILE",
                     help="also write the serving section's full statistics to FILE")
     ap.add_argument("--profile-batch", default=None, metavar="PREC:ORBIT",
-                    help="run only the small batched profiling case (fp64|mixed:equal|kepler)")
+                    help="run only a small batched profiling case (fp64|mixed:equal|kepler|batch64)")
     args = ap.parse_args()
     if args.profile_batch:
         import fastlisaresponse_gb300 as flr

@@ -11,7 +11,7 @@ from ._lib import FLRError, describe_status, library_path
 from . import autotune
 from .batch import BatchedResponseTDI, BatchGraph
 from .binding import LISAResponseWrap, LISAResponseWrapGPU, OrbitsWrap, OrbitsWrapGPU_responselisa
-from .orbits import EqualArmlengthOrbits, KeplerianOrbits, Orbits
+from .orbits import EqualArmlengthOrbits, KeplerianOrbits, Orbits, read_lisa_orbits
 from .serve import Request, ResponseServer
 from .response import (ResponseWrapper, lagrange_tables, pyResponseTDI, sky_basis,
                        tdi_unit_tables)
@@ -25,5 +25,6 @@ __all__ = [
     "LISAResponseWrap", "LISAResponseWrapGPU", "Orbits", "OrbitsWrap",
     "OrbitsWrapGPU_responselisa", "ResponseWrapper", "autotune", "build", "describe_status",
     "gb_waveform", "get_overlap", "lagrange_tables", "library_path", "needs_build",
-    "pyResponseTDI", "Request", "ResponseServer", "sky_basis", "tdi_unit_tables", "time_grid",
+    "pyResponseTDI", "read_lisa_orbits", "Request", "ResponseServer", "sky_basis",
+    "tdi_unit_tables", "time_grid",
 ]

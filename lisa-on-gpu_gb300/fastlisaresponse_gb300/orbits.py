@@ -241,3 +241,36 @@ class KeplerianOrbits(_AnalyticOrbits):
 
     def _evaluate(self, t):
         return _link_tables(self.positions, t, self.armlength / C_SI)
+
+
+def read_lisa_orbits(path, armlength=2.5e9, h5py_module=None) -> Orbits:
+    """Orbits from a LISA Orbits HDF5 file, the files lisatools' ``Orbits``
+    reads for the reference (``response.py:13,119``): the barycentric (TCB)
+    tables ``tcb/x`` (N, 3, 3) spacecraft positions [m], ``tcb/ltt`` (N, 6)
+    light travel times [s] and ``tcb/n`` (N, 6, 3) link unit vectors, links in
+    the order 12, 23, 31, 13, 32, 21, and the root attributes ``dt`` [s] and
+    ``size`` (N); knot i is at i * dt.
+
+    h5py is not a dependency of this package: it is imported here, or pass a
+    module with h5py's ``File`` interface as ``h5py_module``.  The tables can
+    also be read by any other HDF5 reader and given to ``Orbits(t, x, ltt,
+    n)`` directly."""
+    if h5py_module is None:
+        try:
+            import h5py as h5py_module
+        except ImportError as e:
+            raise ImportError("reading LISA Orbits files needs h5py; or read the datasets "
+                              "tcb/x, tcb/ltt, tcb/n with another HDF5 reader and pass them to "
+                              "Orbits(t, x, ltt, n)") from e
+    with h5py_module.File(path, "r") as f:
+        dt = float(f.attrs["dt"])
+        size = int(f.attrs["size"])
+        x = np.asarray(f["tcb"]["x"], dtype=np.float64)
+        ltt = np.asarray(f["tcb"]["ltt"], dtype=np.float64)
+        n = np.asarray(f["tcb"]["n"], dtype=np.float64)
+    if not (dt > 0.0) or size < 2:
+        raise ValueError(f"{path}: bad time grid (dt={dt}, size={size})")
+    if x.shape[0] != size or ltt.shape[0] != size or n.shape[0] != size:
+        raise ValueError(f"{path}: tables do not have `size` = {size} rows")
+    return Orbits(np.arange(size) * dt, x.reshape(size, 3, 3), ltt.reshape(size, 6),
+                  n.reshape(size, 6, 3), armlength)
