@@ -74,7 +74,7 @@ SINGLE = dict(desc="one galactic binary (A 1e-22, f 2e-3 Hz, fdot 1e-14), 1 yr a
               A=1e-22, f=2e-3, fdot=1e-14)
 CPU_SLICE = 2**17         # output samples per CPU task (a slice of one source)
 SUBSET_STRIDE = 16        # plain FP64 leg: every 16th source by length (128 of 2048)
-E2E_GROUP_SAMPLES = 2**27  # samples per launch of the host pipeline
+E2E_GROUP_SAMPLES = 2**25  # samples per launch of the host pipeline
 SINGLE_CHUNKS = 8          # launches per 1 yr step (two streams: last waves overlap)
 SERVE_BATCH_SAMPLES = 2**23
 

@@ -273,7 +273,7 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
                           const flr_tdi_units *sets, int num_sets, int precision, int tile,
                           flr_batch_plan **out);
 int flr_batch_plan_destroy(flr_batch_plan *plan);
-/* info[0..9] = tile, y halo, input window capacity, link row capacity, shared
+/* info[0..11] = tile, y halo, input window capacity, link row capacity, shared
  * memory bytes per block, persistent grid size, precision, 1 when the mixed
  * kernel evaluates the TDI units in equal-delay groups (equal-arm orbits:
  * units with delay lists of equal length share one interpolation of their
@@ -282,7 +282,9 @@ int flr_batch_plan_destroy(flr_batch_plan *plan);
  * small enough; the half-width h when none), and 1 when the mixed kernel
  * evaluates the TDI interpolations in second-difference form (a double-float
  * linear part plus an FP32 sum over second differences; needs the reference's
- * Lagrange tables, else the double-float form is used). */
+ * Lagrange tables, else the double-float form is used), the threads per block
+ * of the fused kernel (256) and its staging depth (input windows in flight
+ * per block: 1).  Fewer entries are written when n_info is smaller. */
 int flr_batch_plan_info(const flr_batch_plan *plan, int *info, int n_info);
 
 /* Test hook (no reference counterpart): the bound, in mbarrier polls, of each

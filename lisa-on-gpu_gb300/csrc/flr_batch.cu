@@ -691,7 +691,8 @@ int flr_batch_plan_info(const flr_batch_plan *plan, int *info, int n_info) {
     const int vals[] = {plan->base.tile, plan->base.y_halo, plan->base.win_max,
                         plan->base.y_max, (int)plan->smem, plan->grid_max,
                         plan->mixed ? FLR_PRECISION_MIXED : FLR_PRECISION_FP64,
-                        plan->grouped ? 1 : 0, plan->base.h_df, plan->base.d2};
+                        plan->grouped ? 1 : 0, plan->base.h_df, plan->base.d2,
+                        flr::kFusedThreads, flr::kFusedStagingDepth};
     for (int i = 0; i < n_info && i < (int)(sizeof(vals) / sizeof(int)); ++i) info[i] = vals[i];
     return FLR_OK;
 }

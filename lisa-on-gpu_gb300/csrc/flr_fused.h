@@ -15,6 +15,11 @@ constexpr int kFusedMaxGroups = kFusedMaxDepth + 1;  // distinct delay-list leng
 // Bound on the mbarrier polls of one staging copy (the default of
 // FusedArgs::wait_polls and the bound of the second wait, see the kernel).
 constexpr long kFusedWaitPolls = 1L << 20;
+// Threads per block of the fused kernel and input windows staged per block
+// (one: an item's window copy is issued when the item starts; measured
+// alternatives are in the plan report's documentation).
+constexpr int kFusedThreads = 256;
+constexpr int kFusedStagingDepth = 1;
 // Status bits of the fused kernel (beside those of flr_device.cuh):
 constexpr unsigned kStatusStaging = 0x10u;      // an item's copy missed its first wait:
                                                 // that item's outputs are NaN

@@ -50,7 +50,7 @@
 namespace flr {
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = kFusedThreads;
 constexpr int kWindowMargin = 4;  // samples added on each side of the window estimate
 
 __device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000ll); }
@@ -118,7 +118,7 @@ __host__ __device__ constexpr size_t align128(size_t x) { return (x + 127) & ~si
 
 __host__ __device__ inline Layout layout(bool mixed, int win_max, int y_max) {
     Layout L{};
-    size_t off = 256;  // mbarrier, scale, window bounds, warp maxima
+    size_t off = 384;  // mbarrier, scale, warp maxima, segment cache, window ends
     L.set = off;
     off = align128(off + sizeof(FusedTdiSet));
     L.edf = off;
@@ -1071,9 +1071,11 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     double *scale_sm = reinterpret_cast<double *>(smem + 16);
     int *scale_exp_sm = reinterpret_cast<int *>(smem + 24);  // scale = 2^(*scale_exp_sm)
-    int *win_sm = reinterpret_cast<int *>(smem + 32);  // [0] = min d, [1] = max d
     SegCache *segc = reinterpret_cast<SegCache *>(smem + 128);  // the item's orbit segments
     double *warp_max = reinterpret_cast<double *>(smem + 64);
+    int2 *ends_sm = reinterpret_cast<int2 *>(smem + 256);  // (min d, max d) per link end
+    static_assert(kThreads / 32 <= 8, "warp maxima: 8 slots");
+    static_assert(sizeof(SegCache) <= 128, "segment cache: 128 bytes");
     FusedTdiSet *set = reinterpret_cast<FusedTdiSet *>(smem + lay.set);
     df::f2 *edf = reinterpret_cast<df::f2 *>(smem + lay.edf);
     double2 *hraw = reinterpret_cast<double2 *>(smem + lay.hraw);
@@ -1095,15 +1097,19 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
     const long num_work = __ldg(a.tile_start + a.num_sources);
     int si = 0;
     for (long wi = blockIdx.x; wi < num_work; wi += gridDim.x) {
-        // source of item wi: the last s with tile_start[s] <= wi (a block's
-        // items only grow, so the search starts at its previous source)
-        int hi = a.num_sources - 1;
-        while (si < hi) {
-            const int mid = (si + hi + 1) >> 1;
-            if (__ldg(a.tile_start + mid) <= wi)
-                si = mid;
-            else
-                hi = mid - 1;
+        // source of item wi: the last s with tile_start[s] <= wi.  A block's
+        // items only grow and mostly stay in one source, so the current
+        // source is checked first; otherwise a binary search from the next.
+        if (__ldg(a.tile_start + si + 1) <= wi) {
+            ++si;
+            int hi = a.num_sources - 1;
+            while (si < hi) {
+                const int mid = (si + hi + 1) >> 1;
+                if (__ldg(a.tile_start + mid) <= wi)
+                    si = mid;
+                else
+                    hi = mid - 1;
+            }
         }
         const long tile_idx = wi - __ldg(a.tile_base + si);
         const FusedSource &src = a.sources[si];
@@ -1152,39 +1158,45 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
         const int Y = (int)(yb - ya);
 
         // 1. input window: delays at both ends of the computed stream range
-        if (tid == 0) {
-            win_sm[0] = 0x7fffffff;
-            win_sm[1] = -0x7fffffff;
-            // the item's times: its link-stream samples, and their emission
-            // times up to 100 s earlier
-            if (kMixed)
-                seg_cache_setup(segc, a.orb, a.inv_orbit_dt, t0 + (double)ya * a.dt - 100.0,
-                                t0 + (double)yb * a.dt);
-        }
-        __syncthreads();
-        if (tid < 12 && yfirst < ylast) {
-            const int slot = tid % 6;
-            const long j = (tid < 6) ? yfirst : ylast - 1;
-            const double t = t0 + (double)j * a.dt;
-            int dr, de;
-            if (kMixed) {
-                MixedDelays g = link_delays_mixed(a.orb, a.inv_orbit_dt, slot, t, t0, a.fs, k);
-                dr = g.d_rec;
-                de = g.d_em;
-            } else {
-                LinkGeometry g = link_geometry(a.orb, slot, t, t0, a.fs, k, u, v);
-                dr = g.d_rec;
-                de = g.d_em;
+        // (threads 0-11, one link end each) and, in parallel, the item's orbit
+        // segments (thread 32: its link-stream times and their emission times
+        // up to 100 s earlier); one barrier for both
+        if (tid < 12) {
+            int2 e = make_int2(0x7fffffff, -0x7fffffff);
+            if (yfirst < ylast) {
+                const int slot = tid % 6;
+                const long j = (tid < 6) ? yfirst : ylast - 1;
+                const double t = t0 + (double)j * a.dt;
+                int dr, de;
+                if (kMixed) {
+                    MixedDelays g = link_delays_mixed(a.orb, a.inv_orbit_dt, slot, t, t0, a.fs, k);
+                    dr = g.d_rec;
+                    de = g.d_em;
+                } else {
+                    LinkGeometry g = link_geometry(a.orb, slot, t, t0, a.fs, k, u, v);
+                    dr = g.d_rec;
+                    de = g.d_em;
+                }
+                e = make_int2(min(dr, de), max(dr, de));
             }
-            atomicMin(&win_sm[0], min(dr, de));
-            atomicMax(&win_sm[1], max(dr, de));
+            ends_sm[tid] = e;
+        } else if (kMixed && tid == 32) {
+            seg_cache_setup(segc, a.orb, a.inv_orbit_dt, t0 + (double)ya * a.dt - 100.0,
+                            t0 + (double)yb * a.dt);
         }
         __syncthreads();
         long wlo = 0;
         int W = 0;
         if (yfirst < ylast) {
-            wlo = max((long)win_sm[0] - (h - 1) - kWindowMargin, 0L);
-            const long whi = min((long)win_sm[1] + h + 1 + kWindowMargin, n);
+            int dmin = 0x7fffffff, dmax = -0x7fffffff;
+#pragma unroll
+            for (int q = 0; q < 12; ++q) {
+                const int2 e = ends_sm[q];
+                dmin = min(dmin, e.x);
+                dmax = max(dmax, e.y);
+            }
+            wlo = max((long)dmin - (h - 1) - kWindowMargin, 0L);
+            const long whi = min((long)dmax + h + 1 + kWindowMargin, n);
             W = (int)max(0L, min(whi - wlo, (long)a.win_max));
         }
 

@@ -129,6 +129,31 @@ GRAPH_WAVEFORMS = 0x1
 GRAPH_DIAGNOSTICS = 0x2
 
 
+def _contiguous_runs(tensors):
+    """Runs of consecutive contiguous tensors that follow each other in one
+    storage: (first index, end index, one flat tensor over the run), so that
+    a run is copied with one cudaMemcpyAsync instead of one per tensor."""
+    runs, k = [], 0
+    while k < len(tensors):
+        first = tensors[k]
+        end = first.data_ptr() + first.numel() * first.element_size()
+        base = first.untyped_storage().data_ptr()
+        count, j = first.numel(), k + 1
+        while j < len(tensors):
+            x = tensors[j]
+            if (x.data_ptr() != end or x.dtype != first.dtype
+                    or x.untyped_storage().data_ptr() != base):
+                break
+            end += x.numel() * x.element_size()
+            count += x.numel()
+            j += 1
+        span = first.reshape(-1) if j == k + 1 else \
+            first.as_strided((count,), (1,), first.storage_offset())
+        runs.append((k, j, span))
+        k = j
+    return runs
+
+
 def _waveform_buffers(h, lengths, device, keep_waveforms):
     """Waveform buffers of a run with generated waveforms: the caller's, new
     ones, or (keep_waveforms False) None for each source: generated inside
@@ -228,12 +253,15 @@ class BatchedResponseTDI:
         _lib.check(rc)
         self._plan = plan
         self._graphs = {}
-        info = (ctypes.c_int * 10)()
-        lib.flr_batch_plan_info(plan, info, 10)
+        info = (ctypes.c_int * 12)()
+        lib.flr_batch_plan_info(plan, info, 12)
         self.plan_info = dict(zip(("tile", "y_halo", "win_max", "y_max", "smem_bytes",
                                    "grid", "precision", "grouped", "fp32_tap_from",
-                                   "tdi_second_differences"),
+                                   "tdi_second_differences", "threads", "staging_depth"),
                                   list(info)))
+        if self.tune is not None:  # the knobs the plan runs with, tuned or fixed
+            self.tune = dict(self.tune, threads=self.plan_info["threads"],
+                             staging_depth=self.plan_info["staging_depth"])
         self._ctor = dict(sampling_frequency=sampling_frequency, order=order, tdi=tdi,
                           orbits=orbits, tdi_chan=tdi_chan, precision=precision,
                           t_buffer=t_buffer, force_backend=self.device)
@@ -381,7 +409,10 @@ class BatchedResponseTDI:
         moves each launch's input (a chunk's with the halo its delays can
         reach), two compute streams with a plan each run the launches (one
         launch's tail overlaps the next one's start) and a second copy stream
-        returns each launch's channels as soon as it is done.  Results are
+        returns each launch's channels as soon as it is done.  A launch of
+        whole sources takes one device buffer for its inputs and one for its
+        channels, and sources adjacent in host memory (consecutive views of
+        one HostArray) move with one copy per run each way.  Results are
         bit-identical to ``__call__`` on device copies of the inputs (sample i
         is at t0 + i dt in every chunk and group).
 
@@ -520,9 +551,58 @@ class BatchedResponseTDI:
         reach = self._reach
         d_h, d_o, done_in = {}, {}, {}
         in_flight = collections.deque()  # completion events of the launches' returns
-        for k, unit in enumerate(self._launch_units(lengths, chunks, group_samples)):
+        units = self._launch_units(lengths, chunks, group_samples)
+        # launches of whole sources take their device buffers from a ring of
+        # four slots, allocated once on the calling stream (every side stream's
+        # work is joined back into it before they are freed): at most three
+        # launches are in flight, so a slot's previous launch has completed
+        # when it is reused, and the loop makes no allocation (an allocation
+        # that cannot reuse a cached block calls cudaMalloc, which waits for
+        # the whole device)
+        whole = [all(r is None for _, r in u) for u in units]
+        ring_n = max([sum(lengths[i] for i, _ in u) for u, w in zip(units, whole) if w],
+                     default=0)
+        if host and ring_n:
+            with torch.cuda.stream(cur):
+                ring_h = [torch.empty(ring_n, dtype=torch.complex128, device=dev)
+                          for _ in range(4)]
+                ring_o = [torch.empty(3 * ring_n, dtype=torch.float64, device=dev)
+                          for _ in range(4)]
+        for k, unit in enumerate(units):
             comp = s_comp[k % 2]
             idx = [i for i, _ in unit]
+            if host and whole[k]:
+                # whole sources: one slot for the launch's inputs and one for its
+                # channels, one copy per run of sources adjacent in host memory
+                # (e.g. views of one HostArray) each way
+                ns_u = [lengths[i] for i in idx]
+                offs = np.concatenate([[0], np.cumsum(ns_u)]).astype(np.int64)
+                buf_h = ring_h[k % 4][:int(offs[-1])]
+                buf_o = ring_o[k % 4][:3 * int(offs[-1])]
+                hs_u = [buf_h[offs[j]:offs[j + 1]] for j in range(len(idx))]
+                outs_u = [buf_o[3 * offs[j]:3 * offs[j + 1]].view(3, ns_u[j])
+                          for j in range(len(idx))]
+                ev_in = torch.cuda.Event()
+                with torch.cuda.stream(s_in):
+                    for a, b, span in _contiguous_runs([host_hs[i] for i in idx]):
+                        buf_h[offs[a]:offs[b]].copy_(span, non_blocking=True)
+                    ev_in.record(s_in)
+                comp.wait_event(ev_in)
+                plans[k % 2]._run(hs_u, None, ns_u, lam[idx], beta[idx], t0[idx], sets[idx],
+                                  outs_u, comp, False, None)
+                ev_k = torch.cuda.Event()
+                ev_k.record(comp)
+                s_out.wait_event(ev_k)
+                with torch.cuda.stream(s_out):
+                    for a, b, span in _contiguous_runs([host_outs[i] for i in idx]):
+                        span.copy_(buf_o[3 * offs[a]:3 * offs[b]], non_blocking=True)
+                    ev_back = torch.cuda.Event()
+                    ev_back.record(s_out)
+                del buf_h, buf_o, hs_u, outs_u
+                in_flight.append(ev_back)
+                if len(in_flight) > 3:
+                    in_flight.popleft().synchronize()
+                continue
             if host:
                 ev_in = torch.cuda.Event()
                 with torch.cuda.stream(s_in):

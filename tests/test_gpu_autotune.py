@@ -26,6 +26,10 @@ def test_auto_tile_tunes_caches_and_matches(gpu_lib, tmp_path, monkeypatch):
     assert r["tile"] in (128, 512) and set(r["timings"]) == {"128", "512"} and not r["cached"]
     bat = flr.BatchedResponseTDI(1 / dt, tile="auto", tune_lengths=lengths, **kw)
     assert bat.tune["cached"] and bat.plan_info["tile"] == r["tile"]
+    # the plan reports the knobs it runs with: the tuned tile, the fixed CTA
+    # size and staging depth
+    assert (bat.tune["threads"], bat.tune["staging_depth"]) == (256, 1)
+    assert (bat.plan_info["threads"], bat.plan_info["staging_depth"]) == (256, 1)
     other = 512 if r["tile"] == 128 else 128
     ref = flr.BatchedResponseTDI(1 / dt, tile=other, **kw)
     hs, lam, beta, t0 = _sources(orb, dt, lengths, seed=9)

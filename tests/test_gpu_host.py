@@ -77,6 +77,44 @@ def test_run_host_groups_short_sources(gpu_lib, precision):
     assert bat.status() == 0
 
 
+def test_run_host_adjacent_views_share_copies(gpu_lib):
+    """Sources that are consecutive views of one HostArray (inputs and
+    channels) are moved with one copy per launch each way; same bits as one
+    device run, including a gap that breaks the run."""
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+    from fastlisaresponse_gb300.batch import _contiguous_runs
+
+    dt = 10.0
+    orb = flr.EqualArmlengthOrbits(t_max=1.6e6)
+    lengths = [2300, 5000, 41000, 3000, 12345, 9000]
+    hs, lam, beta, t0 = _sources(orb, dt, lengths, seed=53)
+    bat = flr.BatchedResponseTDI(1 / dt, tdi="2nd generation", orbits=orb, precision="mixed")
+    want = [_np(o) for o in bat(hs, lam, beta, t0=t0)]
+    tot = sum(lengths) + 7  # a gap of 7 samples after the third source
+    h_all = flr.HostArray(tot, np.complex128)
+    o_all = flr.HostArray(3 * tot)
+    try:
+        h_v, o_v, off = [], [], 0
+        for j, (n, x) in enumerate(zip(lengths, hs)):
+            h_v.append(h_all.tensor[off:off + n])
+            h_v[-1].copy_(torch.from_numpy(np.asarray(x)))
+            o_v.append(o_all.tensor[3 * off:3 * (off + n)].view(3, n))
+            off += n + (7 if j == 2 else 0)
+        assert [(a, b) for a, b, _ in _contiguous_runs(h_v)] == [(0, 3), (3, 6)]
+        assert [(a, b) for a, b, _ in _contiguous_runs(o_v)] == [(0, 3), (3, 6)]
+        o_all.array.fill(np.nan)
+        got = bat.run_host(h_v, lam, beta, t0=t0, out=o_v, group_samples=10**9)
+        torch.cuda.synchronize(bat.device)
+        for g, w in zip(got, want):
+            assert np.array_equal(g.numpy(), w)
+    finally:
+        h_all.release()
+        o_all.release()
+    assert bat.status() == 0
+
+
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_chunked_device_call_matches_one_launch(gpu_lib, precision):
     """__call__(chunks=k): tile-aligned launches over two streams, same bits."""
