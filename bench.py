@@ -916,18 +916,35 @@ def run_reference(args):
 
 
 def run_profile_batch(spec: str) -> None:
-    """Small batched cases for ncu captures, spec = "<fp64|mixed>:<kind>":
+    """Small cases for ncu captures, spec = "<fp64|mixed|plain>:<kind>":
     kind equal|kepler: 16 galactic binaries x 2^18 samples at dt = 10 s with
     equal-arm or Keplerian orbits; kind batch64: the first 64 sources of the
     batching configuration (49.3 M samples, 2.0 GB of inputs and outputs).
-    2nd-gen TDI XYZ, order 25.  Two calls of the batch (the capture takes the
-    first)."""
+    2nd-gen TDI XYZ, order 25; plain:<equal|kepler>: the plain FP64 drop-in
+    path (pyResponseTDI) on one source of 2^21 samples at dt = 5 s.  Two
+    calls (the capture takes the first)."""
     import torch
 
     import fastlisaresponse_gb300 as flr
 
     prec, kind = spec.split(":")
     dev = torch.device("cuda", 0)
+    if prec == "plain":
+        # the plain FP64 drop-in path on one source of 2^21 samples at dt = 5 s
+        dt, n = 5.0, 2**21
+        orb = flr.EqualArmlengthOrbits(t_max=orbit_t_max(n, dt)) if kind == "equal" else \
+            flr.KeplerianOrbits(t_max=orbit_t_max(n, dt))
+        h = flr.gb_waveform(SINGLE["A"], SINGLE["f"], SINGLE["fdot"], 0.7, 0.3, 0.2,
+                            torch.arange(n, dtype=torch.float64, device=dev) * dt)
+        resp = flr.pyResponseTDI(1 / dt, n, order=25, tdi="2nd generation", orbits=orb,
+                                 force_backend=dev)
+        for _ in range(2):
+            resp.get_projections(h, 1.0, 0.3, t_buffer=T_BUFFER)
+            resp.get_tdi_delays()
+        torch.cuda.synchronize()
+        assert resp.status() == 0
+        print(json.dumps({"profile_batch": spec, "computed_samples": n - 2 * resp.tdi_start_ind}))
+        return
     dt = 10.0
     if kind == "batch64":
         lengths, p = batch_sources(BATCH["sources"])
@@ -974,7 +991,7 @@ def main():
     ap.add_argument("--details", default=None, metavar="FILE",
                     help="also write the serving section's full statistics to FILE")
     ap.add_argument("--profile-batch", default=None, metavar="PREC:ORBIT",
-                    help="run only a small batched profiling case (fp64|mixed:equal|kepler|batch64)")
+                    help="run only a small profiling case (fp64|mixed:equal|kepler|batch64, plain:equal|kepler)")
     args = ap.parse_args()
     if args.profile_batch:
         import fastlisaresponse_gb300 as flr

@@ -146,7 +146,10 @@ int flr_get_response(flr_orbits *orbits, double *y_gw, const double *t_data, con
  *   tdi_link_combinations (the kernel cannot check it: the array's length is
  *   not an argument, as in the reference).
  * Unlike the reference GPU kernel (atomicAdd, LISAResponse.cu:389) the sum over
- * units is in a fixed order, so results are deterministic.
+ * units is in a fixed order, so results are deterministic.  With up to three
+ * channels one thread takes all channels of a sample (the six L(t) once, the
+ * sample's tap windows read by one thread); with more, one thread per
+ * (sample, channel).
  */
 int flr_get_tdi_delays(flr_orbits *orbits, double *delayed_links, const double *input_links,
                        int num_inputs, int num_delays, const double *t_arr,
@@ -156,6 +159,24 @@ int flr_get_tdi_delays(flr_orbits *orbits, double *delayed_links, const double *
                        double sampling_frequency, int buffer_integer, const double *A_in,
                        double deps, int num_A, const double *E_in, int tdi_start_ind,
                        void *stream);
+
+/*
+ * flr_get_tdi_delays followed, in the same kernel, by the A, E (and T) of
+ * flr_xyz_to_aet (below) of the accumulated X, Y, Z: needs num_channels 3;
+ * aet [aet_rows][num_delays], aet_rows 3 (A, E, T) or 2 (A, E); the samples
+ * [tdi_start_ind, num_delays - tdi_start_ind) are written, delayed_links as
+ * flr_get_tdi_delays writes it.  The reference forms AET on the host after
+ * the TDI call (response.py:659-673).
+ */
+int flr_get_tdi_delays_aet(flr_orbits *orbits, double *delayed_links, const double *input_links,
+                           int num_inputs, int num_delays, const double *t_arr,
+                           const int *unit_starts, const int *unit_lengths,
+                           const int *tdi_base_link, const int *tdi_link_combinations,
+                           const double *tdi_signs, const int *channels, int num_units,
+                           int num_channels, int order, double sampling_frequency,
+                           int buffer_integer, const double *A_in, double deps, int num_A,
+                           const double *E_in, int tdi_start_ind, double *aet, int aet_rows,
+                           void *stream);
 
 /*
  * Diagnostics: the integer delay indices the two kernels above compute, from

@@ -243,7 +243,7 @@ bool fit_sigma_table(const std::vector<double> &A, const std::vector<double> &E,
 // Staging layout: descriptors | tile prefix sums | waveform parameters |
 // chunk prefix sums, each part 256-byte aligned.
 struct StageLayout {
-    size_t tiles, base, gb, chunks, bytes;
+    size_t tiles, base, gb, chunks, counter, bytes;
 };
 
 StageLayout stage_layout(int cap, bool waveforms) {
@@ -253,7 +253,8 @@ StageLayout stage_layout(int cap, bool waveforms) {
     l.base = up(l.tiles + sizeof(long) * ((size_t)cap + 1));
     l.gb = up(l.base + sizeof(long) * ((size_t)cap + 1));
     l.chunks = up(l.gb + (waveforms ? sizeof(flr::GbParams) * (size_t)cap : 0));
-    l.bytes = l.chunks + (waveforms ? sizeof(long) * ((size_t)cap + 1) : 0);
+    l.counter = up(l.chunks + (waveforms ? sizeof(long) * ((size_t)cap + 1) : 0));
+    l.bytes = l.counter + sizeof(unsigned long long);
     return l;
 }
 
@@ -350,6 +351,8 @@ int fill_stage(const flr_batch_plan *plan, const flr_batch_source *sources, int 
         tile_base[i] = tiles;
         if (gb) chunk_start[i] = chunks;
     }
+    // the work-item counter starts at zero in every run (the copy resets it)
+    *reinterpret_cast<unsigned long long *>(hs + lay.counter) = 0ull;
     return FLR_OK;
 }
 
@@ -372,6 +375,7 @@ cudaError_t enqueue(const flr_batch_plan *plan, const unsigned char *h_stage,
     a.sources = d_src;
     a.tile_start = reinterpret_cast<const long *>(d_stage + lay.tiles);
     a.tile_base = reinterpret_cast<const long *>(d_stage + lay.base);
+    a.work_next = reinterpret_cast<unsigned long long *>(d_stage + lay.counter);
     a.num_sources = cap;
     a.chan = chan;
     a.partial = partial;

@@ -225,15 +225,14 @@ int flr_get_response(flr_orbits *orbits, double *y_gw, const double *t_data, con
     return FLR_OK;
 }
 
-int flr_get_tdi_delays(flr_orbits *orbits, double *delayed_links, const double *input_links,
-                       int num_inputs, int num_delays, const double *t_arr,
-                       const int *unit_starts, const int *unit_lengths, const int *tdi_base_link,
-                       const int *tdi_link_combinations, const double *tdi_signs,
-                       const int *channels, int num_units, int num_channels, int order,
-                       double sampling_frequency, int buffer_integer, const double *A_in,
-                       double deps, int num_A, const double *E_in, int tdi_start_ind,
-                       void *stream) {
-    (void)buffer_integer;
+static int tdi_delays(flr_orbits *orbits, double *delayed_links, const double *input_links,
+                      int num_inputs, int num_delays, const double *t_arr,
+                      const int *unit_starts, const int *unit_lengths, const int *tdi_base_link,
+                      const int *tdi_link_combinations, const double *tdi_signs,
+                      const int *channels, int num_units, int num_channels, int order,
+                      double sampling_frequency, const double *A_in, double deps, int num_A,
+                      const double *E_in, int tdi_start_ind, double *aet, int aet_rows,
+                      void *stream) {
     g_last_error.clear();
     int rc = check_device(orbits);
     if (rc) return rc;
@@ -246,6 +245,10 @@ int flr_get_tdi_delays(flr_orbits *orbits, double *delayed_links, const double *
     if (num_delays < 1 || num_inputs < 1 || tdi_start_ind < 0 || num_units < 0 ||
         num_channels < 0 || num_channels > 65535)
         return fail(FLR_E_INVALID_ARGUMENT, "invalid sizes");
+    if (aet && (num_channels != 3 || (aet_rows != 2 && aet_rows != 3)))
+        return fail(FLR_E_INVALID_ARGUMENT, "A, E, T need num_channels 3 and aet_rows 2 or 3");
+    a.aet = aet;
+    a.aet_rows = aet ? aet_rows : 0;
     if (!(sampling_frequency > 0.0))
         return fail(FLR_E_INVALID_ARGUMENT, "sampling_frequency must be positive");
     a.orb = flr::device_tables(orbits);
@@ -267,6 +270,38 @@ int flr_get_tdi_delays(flr_orbits *orbits, double *delayed_links, const double *
     cudaError_t err = flr::launch_tdi_plain(a, static_cast<cudaStream_t>(stream));
     if (err != cudaSuccess) return cuda_fail(err, "launching the TDI kernel");
     return FLR_OK;
+}
+
+int flr_get_tdi_delays(flr_orbits *orbits, double *delayed_links, const double *input_links,
+                       int num_inputs, int num_delays, const double *t_arr,
+                       const int *unit_starts, const int *unit_lengths, const int *tdi_base_link,
+                       const int *tdi_link_combinations, const double *tdi_signs,
+                       const int *channels, int num_units, int num_channels, int order,
+                       double sampling_frequency, int buffer_integer, const double *A_in,
+                       double deps, int num_A, const double *E_in, int tdi_start_ind,
+                       void *stream) {
+    (void)buffer_integer;
+    return tdi_delays(orbits, delayed_links, input_links, num_inputs, num_delays, t_arr,
+                      unit_starts, unit_lengths, tdi_base_link, tdi_link_combinations, tdi_signs,
+                      channels, num_units, num_channels, order, sampling_frequency, A_in, deps,
+                      num_A, E_in, tdi_start_ind, nullptr, 0, stream);
+}
+
+int flr_get_tdi_delays_aet(flr_orbits *orbits, double *delayed_links, const double *input_links,
+                           int num_inputs, int num_delays, const double *t_arr,
+                           const int *unit_starts, const int *unit_lengths,
+                           const int *tdi_base_link, const int *tdi_link_combinations,
+                           const double *tdi_signs, const int *channels, int num_units,
+                           int num_channels, int order, double sampling_frequency,
+                           int buffer_integer, const double *A_in, double deps, int num_A,
+                           const double *E_in, int tdi_start_ind, double *aet, int aet_rows,
+                           void *stream) {
+    (void)buffer_integer;
+    if (!aet) return fail(FLR_E_INVALID_ARGUMENT, "aet must not be NULL");
+    return tdi_delays(orbits, delayed_links, input_links, num_inputs, num_delays, t_arr,
+                      unit_starts, unit_lengths, tdi_base_link, tdi_link_combinations, tdi_signs,
+                      channels, num_units, num_channels, order, sampling_frequency, A_in, deps,
+                      num_A, E_in, tdi_start_ind, aet, aet_rows, stream);
 }
 
 int flr_response_delay_indices(flr_orbits *orbits, int *d_rec, int *d_em, const double *t_data,

@@ -105,6 +105,11 @@ struct FusedArgs {
     // tile_base[s] = tile_start[s] - (index of the first tile source s computes),
     // so that work item w is tile w - tile_base[s] of its source
     const long *tile_base;
+    // Work items after each block's first (blockIdx.x) are taken from this
+    // counter in the staged image (zero when staged): item gridDim.x + the
+    // counter's old value.  A block that runs faster takes more items, so no
+    // SM idles while others finish.  NULL: static striding by gridDim.x.
+    unsigned long long *work_next;
     int num_sources;
     // per work item: the six partial inner products of its tile (inner-product
     // runs only; reduced per source by launch_inner_reduce)

@@ -843,22 +843,11 @@ __device__ __forceinline__ df::f2 d2_interp_real(const float2 *y, const float *d
     return d2_combine(l, w, acc);
 }
 
-// The grouped form: the same weights for the virtual rows of the three
-// channels (offsets off[c] into y / dd, signs sg[c], 0 = no term).
-__device__ __forceinline__ void d2_interp_group(const float2 *y, const float *dd, const int off[3],
-                                                const float sg[3], int d, df::f2 e,
-                                                const D2Weights &w, const df::f2 *edf, int h,
-                                                df::f2 out[3]) {
-    const df::f2 ome = df::one_minus(e);
-    const float e32 = e.hi, o32 = ome.hi + ome.lo, c = e32 * o32;
+// The partial sums (UR_j, UL_j), j = h-1 .. 1, of the grouped form's FP32
+// remainder weights: functions of e32 (eps rounded to FP32) alone.
+__device__ __forceinline__ void d2_group_sums(float e32, const df::f2 *edf, int h, float2 *tab) {
+    const float o32 = 1.0f - e32, c = e32 * o32;
     float R = 0.f, UR = 0.f, L = 0.f, UL = 0.f;
-    float acc[3] = {0.f, 0.f, 0.f};
-    const float *up[3], *dn[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        up[k] = dd + off[k] + d + h - 1;
-        dn[k] = dd + off[k] + d + 2 - h;
-    }
     const df::f2 *Ej = edf + h - 2;
     float jf = (float)(h - 1);
     for (int j = h - 1; j >= 1; --j, --Ej, jf -= 1.f) {
@@ -867,10 +856,49 @@ __device__ __forceinline__ void d2_interp_group(const float2 *y, const float *dd
         UR += R;
         L = __fmaf_rn(cE, df::rcp_approx(jf + o32), L);
         UL += L;
-        const int o = h - 1 - j;
+        tab[h - 1 - j] = make_float2(UR, UL);
+    }
+}
+
+// The grouped form: the same weights for the virtual rows of the three
+// channels (offsets off[c] into y / dd, signs sg[c], 0 = no term).  tab: the
+// partial sums of d2_group_sums for this e32 when the caller has them (the
+// same values), else nullptr.
+__device__ __forceinline__ void d2_interp_group(const float2 *y, const float *dd, const int off[3],
+                                                const float sg[3], int d, df::f2 e,
+                                                const D2Weights &w, const df::f2 *edf, int h,
+                                                const float2 *tab, df::f2 out[3]) {
+    const df::f2 ome = df::one_minus(e);
+    float acc[3] = {0.f, 0.f, 0.f};
+    const float *up[3], *dn[3];
 #pragma unroll
-        for (int k = 0; k < 3; ++k)
-            acc[k] = __fmaf_rn(UL, dn[k][o], __fmaf_rn(UR, up[k][-o], acc[k]));
+    for (int k = 0; k < 3; ++k) {
+        up[k] = dd + off[k] + d + h - 1;
+        dn[k] = dd + off[k] + d + 2 - h;
+    }
+    if (tab != nullptr) {
+        for (int o = 0; o < h - 1; ++o) {
+            const float2 u = tab[o];
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                acc[k] = __fmaf_rn(u.y, dn[k][o], __fmaf_rn(u.x, up[k][-o], acc[k]));
+        }
+    } else {
+        const float e32 = e.hi, o32 = 1.0f - e32, c = e32 * o32;
+        float R = 0.f, UR = 0.f, L = 0.f, UL = 0.f;
+        const df::f2 *Ej = edf + h - 2;
+        float jf = (float)(h - 1);
+        for (int j = h - 1; j >= 1; --j, --Ej, jf -= 1.f) {
+            const float cE = c * Ej->hi;
+            R = __fmaf_rn(cE, df::rcp_approx(jf + e32), R);
+            UR += R;
+            L = __fmaf_rn(cE, df::rcp_approx(jf + o32), L);
+            UL += L;
+            const int o = h - 1 - j;
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                acc[k] = __fmaf_rn(UL, dn[k][o], __fmaf_rn(UR, up[k][-o], acc[k]));
+        }
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -1074,6 +1102,7 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
     SegCache *segc = reinterpret_cast<SegCache *>(smem + 128);  // the item's orbit segments
     double *warp_max = reinterpret_cast<double *>(smem + 64);
     int2 *ends_sm = reinterpret_cast<int2 *>(smem + 256);  // (min d, max d) per link end
+    long long *next_sm = reinterpret_cast<long long *>(smem + 352);  // next item, 2 slots
     static_assert(kThreads / 32 <= 8, "warp maxima: 8 slots");
     static_assert(sizeof(SegCache) <= 128, "segment cache: 128 bytes");
     FusedTdiSet *set = reinterpret_cast<FusedTdiSet *>(smem + lay.set);
@@ -1096,7 +1125,15 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
     int loaded_set = -1;
     const long num_work = __ldg(a.tile_start + a.num_sources);
     int si = 0;
-    for (long wi = blockIdx.x; wi < num_work; wi += gridDim.x) {
+    int par = 0;  // slot of next_sm this item's successor is written to
+    // The block's next item is fetched by thread 0 at the start of an item and
+    // read by all after the item's last barrier (the loop increment; a
+    // `continue` passes through it too); the two slots alternate, so a slot
+    // is rewritten only after every thread has read it.
+    for (long wi = blockIdx.x; wi < num_work; wi = next_sm[par], par ^= 1) {
+        if (tid == 0)
+            next_sm[par] = a.work_next ? (long long)gridDim.x + (long long)atomicAdd(a.work_next, 1ull)
+                                       : wi + gridDim.x;
         // source of item wi: the last s with tile_start[s] <= wi.  A block's
         // items only grow and mostly stay in one source, so the current
         // source is checked first; otherwise a binary search from the next.
@@ -1640,8 +1677,40 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
         }
         // 4c. second-difference form: the rows' second differences (the input
         // window's space is free now)
+        // Equal-delay groups: a group's delay has the same fractional part at
+        // every sample up to FP64 rounding (equal arms), so its eps rounded to
+        // FP32 (what the FP32 remainder weights depend on) takes one value or
+        // a neighbour of it across a tile.  The partial sums are tabulated
+        // for the first output sample's value and its two FP32 neighbours;
+        // samples with one of those values read them, the others compute
+        // them: the same numbers either way.  The tables sit behind the
+        // second differences in the input window's space.
+        const size_t tab_off = lay.d2 + align128(sizeof(float) * 6 * (size_t)a.y_max);
+        float *wkey = reinterpret_cast<float *>(smem + tab_off);
+        float2 *wtab = reinterpret_cast<float2 *>(smem + tab_off + 256);
+        const bool use_tab = kGrouped && kD2 && o0 < o1 &&
+                             tab_off + 256 + sizeof(float2) * 3 * kFusedMaxGroups * (h - 1) <=
+                                 lay.y;
         if (kMixed && kD2) {
             second_differences(y32, d2, kGrouped ? set->num_vrows : 6, Y, a.y_max, tid, kThreads);
+            if (use_tab && tid < 3 * set->num_groups) {
+                const int g = tid / 3, v = tid - 3 * g;
+                const double t = t0 + (double)o0 * a.dt;
+                const Seg w = seg_of(segc, a.orb, a.inv_orbit_dt, t);
+                const double L0 =
+                    (w.w < 0) ? 0.0
+                              : orbit_lerp_b(a.orb.ltt, a.orb.ltt_slope, w.w, 6, 0, t, w.base);
+                double delay = t;
+                for (int m = 0; m < set->group_len[g]; ++m) delay = delay - L0;
+                int d;
+                df::f2 e;
+                split_delay_df(delay, t0, a.fs, d, e);
+                // the neighbours of a non-negative float by its bits (below 0: a
+                // NaN key, which no sample matches)
+                const float key = __int_as_float(__float_as_int(e.hi) + (v - 1));
+                wkey[tid] = key;
+                d2_group_sums(key, edf, h, wtab + (size_t)tid * (h - 1));
+            }
             __syncthreads();
         }
 
@@ -1686,7 +1755,17 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
                     df::f2 val[3];
                     if (kD2) {
                         const D2Weights w2 = d2_weights(a, inv_deps_df, e_df);
-                        d2_interp_group(y32, d2, off, sg, (int)(d - ya), e_df, w2, edf, h, val);
+                        const float2 *tab = nullptr;
+                        if (use_tab) {
+                            const float k32 = e_df.hi;
+                            const int q = (k32 == wkey[3 * g + 1])   ? 3 * g + 1
+                                          : (k32 == wkey[3 * g])     ? 3 * g
+                                          : (k32 == wkey[3 * g + 2]) ? 3 * g + 2
+                                                                     : -1;
+                            if (q >= 0) tab = wtab + (size_t)q * (h - 1);
+                        }
+                        d2_interp_group(y32, d2, off, sg, (int)(d - ya), e_df, w2, edf, h, tab,
+                                        val);
                     } else {
                         const df::f2 A_df = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_df);
                         df_interp_group(y32, off, sg, (int)(d - ya), A_df, e_df, edf, h, a.h_df,

@@ -56,6 +56,10 @@ struct TdiArgs {
     int num_channels;
     double fs;
     int start;               // tdi_start_ind
+    // optional epilogue (num_channels == 3): A, E, T (aet_rows 3) or A, E (2)
+    // of the accumulated X, Y, Z, [aet_rows][num_delays]; NULL: none
+    double *aet = nullptr;
+    int aet_rows = 0;
 };
 
 cudaError_t launch_response_plain(const ResponseArgs &a, cudaStream_t stream);

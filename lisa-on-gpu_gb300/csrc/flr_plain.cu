@@ -76,8 +76,10 @@ response_plain_kernel(ResponseArgs a) {
     *out = pre * big;
 }
 
+// One thread per (sample, channel), the channel rows of a tile in
+// consecutive blocks: for more than three channels.
 __global__ void __launch_bounds__(kThreads)
-tdi_plain_kernel(TdiArgs a) {
+tdi_plain_channel_kernel(TdiArgs a) {
     const int channel = (int)(blockIdx.x % (unsigned)a.num_channels);
     const long i =
         (long)a.start + (long)(blockIdx.x / (unsigned)a.num_channels) * kThreads + threadIdx.x;
@@ -195,14 +197,98 @@ unsigned interleaved_grid(long count, int rows) {
 // (X + Y + Z)/sqrt3, in NumPy's operation order with correctly rounded
 // division (the values of the reference's AET on the same XYZ); `rows` = 2
 // writes A and E only.
+__device__ __forceinline__ void store_aet(double *aet, long n, long i, int rows, double X,
+                                          double Y, double Z) {
+    aet[i] = (Z - X) / 1.4142135623730951;
+    aet[n + i] = (X - 2.0 * Y + Z) / 2.449489742783178;
+    if (rows > 2) aet[2 * n + i] = (X + Y + Z) / 1.7320508075688772;
+}
+
 __global__ void __launch_bounds__(kThreads)
 xyz_to_aet_kernel(const double *xyz, double *aet, long n, long start, int rows) {
     const long i = start + (long)blockIdx.x * kThreads + threadIdx.x;
     if (i >= n - start) return;
-    const double X = xyz[i], Y = xyz[n + i], Z = xyz[2 * n + i];
-    aet[i] = (Z - X) / 1.4142135623730951;
-    aet[n + i] = (X - 2.0 * Y + Z) / 2.449489742783178;
-    if (rows > 2) aet[2 * n + i] = (X + Y + Z) / 1.7320508075688772;
+    store_aet(aet, n, i, rows, xyz[i], xyz[n + i], xyz[2 * n + i]);
+}
+
+// One thread per sample and all (at most three) channels: the six L(t) once
+// per sample, each unit's interpolation added to its channel in unit order
+// (the per-channel sums of the reference, bit for bit), the tap windows of a
+// sample read by one thread; optional A, E, T epilogue.
+__global__ void __launch_bounds__(kThreads)
+tdi_plain_kernel(TdiArgs a) {
+    const long i = (long)a.start + (long)blockIdx.x * kThreads + threadIdx.x;
+    if (i >= a.num_delays - a.start) return;
+
+    const double t = __ldg(a.t_arr + i);
+    const double t_first = __ldg(a.t_arr);
+    // L(t) of every link slot; the reference re-evaluates the same
+    // interpolation for each list entry (LISAResponse.cu:331), which yields
+    // these values.
+    double L[kLinks];
+#pragma unroll
+    for (int s = 0; s < kLinks; ++s) L[s] = light_travel_time(a.orb, t, s);
+
+    const int nc = a.num_channels;
+    const size_t nd = (size_t)a.num_delays;
+    double acc0 = a.out[i];
+    double acc1 = (nc > 1) ? a.out[nd + i] : 0.0;
+    double acc2 = (nc > 2) ? a.out[2 * nd + i] : 0.0;
+    const int h = a.lt.h;
+    for (int unit = 0; unit < a.num_units; ++unit) {
+        const int ch = __ldg(a.channels + unit);
+        if (ch < 0 || ch >= nc) {
+            raise_status(a.orb.status, kStatusChannel);
+            continue;
+        }
+        double delay = t;
+        bool link_ok = true;
+        const int s0 = __ldg(a.unit_starts + unit), n_s = __ldg(a.unit_lengths + unit);
+        for (int s = 0; s < n_s; ++s) {
+            const int link = __ldg(a.combos + s0 + s);
+            if (link == kNoLink) continue;
+            const int slot = link_slot(a.orb, link);
+            if (slot < 0) {
+                link_ok = false;
+                break;
+            }
+            delay -= L[slot];
+        }
+        const int base = link_slot(a.orb, __ldg(a.base_link + unit));
+        double val;
+        if (!link_ok || base < 0) {
+            raise_status(a.orb.status, kStatusLink);
+            val = quiet_nan();
+        } else {
+            int d;
+            double eps, pre;
+            split_delay(delay, t_first, a.fs, d, eps);
+            if ((long)d - (h - 1) < 0 || (long)d + h >= a.num_inputs) {
+                raise_status(a.orb.status, kStatusTap);
+                val = quiet_nan();
+            } else if (!prefactor(a.lt, eps, pre)) {
+                raise_status(a.orb.status, kStatusAIndex);
+                val = quiet_nan();
+            } else {
+                const GlobalF64 row{a.y + (size_t)base * a.num_inputs};
+                val = lagrange_real(row, d, eps, pre, a.lt);
+                val *= __ldg(a.signs + unit);
+            }
+        }
+        // an invalid unit makes its channel NaN (assigned, as the per-channel
+        // form does; NaN stays NaN under later additions)
+        const bool bad = val != val;
+        if (ch == 0)
+            acc0 = bad ? val : acc0 + val;
+        else if (ch == 1)
+            acc1 = bad ? val : acc1 + val;
+        else
+            acc2 = bad ? val : acc2 + val;
+    }
+    a.out[i] = acc0;
+    if (nc > 1) a.out[nd + i] = acc1;
+    if (nc > 2) a.out[2 * nd + i] = acc2;
+    if (a.aet) store_aet(a.aet, a.num_delays, i, a.aet_rows, acc0, acc1, acc2);
 }
 
 }  // namespace
@@ -217,7 +303,11 @@ cudaError_t launch_response_plain(const ResponseArgs &a, cudaStream_t stream) {
 cudaError_t launch_tdi_plain(const TdiArgs &a, cudaStream_t stream) {
     long count = a.num_delays - 2L * a.start;
     if (count <= 0 || a.num_channels <= 0) return cudaSuccess;
-    tdi_plain_kernel<<<interleaved_grid(count, a.num_channels), kThreads, 0, stream>>>(a);
+    if (a.num_channels <= 3)
+        tdi_plain_kernel<<<interleaved_grid(count, 1), kThreads, 0, stream>>>(a);
+    else
+        tdi_plain_channel_kernel<<<interleaved_grid(count, a.num_channels), kThreads, 0,
+                                   stream>>>(a);
     return cudaGetLastError();
 }
 

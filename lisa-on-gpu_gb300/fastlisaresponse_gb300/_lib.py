@@ -50,6 +50,8 @@ _SIGNATURES = {
                                 _i, _p, _d, _i, _p, _i, _p]),
     "flr_response_delay_indices": (_i, [_p, _p, _p, _p, _p, _i, _d, _i, _p]),
     "flr_tdi_delay_indices": (_i, [_p, _p, _i, _p, _p, _p, _p, _i, _d, _i, _p]),
+    "flr_get_tdi_delays_aet": (_i, [_p, _p, _p, _i, _i, _p, _p, _p, _p, _p, _p, _p, _i, _i, _i,
+                                    _d, _i, _p, _d, _i, _p, _i, _p, _i, _p]),
     "flr_xyz_to_aet": (_i, [_p, _p, _i, _i, _i, _p]),
 }
 

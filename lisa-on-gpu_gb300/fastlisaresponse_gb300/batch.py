@@ -285,7 +285,7 @@ class BatchedResponseTDI:
 
     def __call__(self, h: Sequence, lam, beta, t0=0.0, tdi_set=0, out: Optional[Sequence] = None,
                  stream=None, diagnostics: bool = False, use_graph: bool = False,
-                 chunks: int = 1):
+                 chunks: int = 1, group_samples: Optional[int] = None):
         """Evaluate the batch.
 
         Args:
@@ -305,6 +305,10 @@ class BatchedResponseTDI:
                 launches alternating over two streams (and two plans), so that
                 one launch's last wave overlaps the next one's start; the same
                 bits as one launch.  For few, long sources.
+            group_samples: with many sources, launches of about this many
+                samples over runs of consecutive sources (longer sources are
+                split into ``chunks`` pieces), alternating over the two
+                streams as with ``chunks``; the same bits as one launch.
         Returns:
             list of (3, n) tensors: rows X, Y, Z (or A, E, T / A, E and a
             zero third row); samples within t_buffer of either end are zero.
@@ -314,10 +318,11 @@ class BatchedResponseTDI:
         dev = self.device
         hs = [_as_device(x, dev, torch.complex128) for x in h]
         lengths = [len(x) for x in hs]
-        if chunks > 1 and not (diagnostics or use_graph):
+        if (chunks > 1 or group_samples) and not (diagnostics or use_graph):
             outs = list(out) if out is not None else [
                 torch.empty((3, n), dtype=torch.float64, device=dev) for n in lengths]
-            self._pipeline(hs, None, outs, None, lam, beta, t0, tdi_set, chunks, stream)
+            self._pipeline(hs, None, outs, None, lam, beta, t0, tdi_set, chunks, stream,
+                           group_samples=group_samples)
             return outs
         return self._run(hs, None, lengths, lam, beta, t0, tdi_set, out, stream, diagnostics,
                          self._bucket(len(hs), False, diagnostics) if use_graph else None)

@@ -221,8 +221,11 @@ class LISAResponseWrap:
                             unit_starts, unit_lengths, tdi_base_link, tdi_link_combinations,
                             tdi_signs_in, channels, num_units, num_channels, order,
                             sampling_frequency, buffer_integer, A_in, deps, num_A, E_in,
-                            tdi_start_ind):
-        """TDI combinations; argument list of binding_flr.cxx:16-35."""
+                            tdi_start_ind, aet=None, aet_rows=3):
+        """TDI combinations; argument list of binding_flr.cxx:16-35.  With
+        ``aet`` (an addition: a float64 array of aet_rows x num_delays), the
+        same kernel also writes A, E (, T) of the accumulated X, Y, Z
+        (flr_get_tdi_delays_aet)."""
         num_inputs, num_delays, num_units, num_A = (int(num_inputs), int(num_delays),
                                                     int(num_units), int(num_A))
         out = _Array(delayed_links, np.float64, "delayed_links").check_length(num_delays, 3)
@@ -238,11 +241,19 @@ class LISAResponseWrap:
         E = _Array(E_in, np.float64, "E_in").check_min(max(int((order + 1) / 2) - 1, 0))
         out.check_min(int(num_channels) * num_delays)
         self._check_unit_tables(us, ul, bl, lc, sg, ch, num_units, int(num_channels))
-        rc = _lib.lib().flr_get_tdi_delays(
-            self.orbits.handle, out.ptr, y.ptr, num_inputs, num_delays, t.ptr, us.ptr, ul.ptr,
-            bl.ptr, lc.ptr, sg.ptr, ch.ptr, num_units, int(num_channels), int(order),
-            float(sampling_frequency), int(buffer_integer), A.ptr, float(deps), num_A, E.ptr,
-            int(tdi_start_ind), _stream_for(out))
+        if aet is None:
+            rc = _lib.lib().flr_get_tdi_delays(
+                self.orbits.handle, out.ptr, y.ptr, num_inputs, num_delays, t.ptr, us.ptr,
+                ul.ptr, bl.ptr, lc.ptr, sg.ptr, ch.ptr, num_units, int(num_channels), int(order),
+                float(sampling_frequency), int(buffer_integer), A.ptr, float(deps), num_A, E.ptr,
+                int(tdi_start_ind), _stream_for(out))
+        else:
+            ae = _Array(aet, np.float64, "aet").check_length(num_delays, int(aet_rows))
+            rc = _lib.lib().flr_get_tdi_delays_aet(
+                self.orbits.handle, out.ptr, y.ptr, num_inputs, num_delays, t.ptr, us.ptr,
+                ul.ptr, bl.ptr, lc.ptr, sg.ptr, ch.ptr, num_units, int(num_channels), int(order),
+                float(sampling_frequency), int(buffer_integer), A.ptr, float(deps), num_A, E.ptr,
+                int(tdi_start_ind), ae.ptr, int(aet_rows), _stream_for(out))
         _lib.check(rc)
 
     # -- diagnostics (no reference counterpart) ---------------------------------

@@ -441,26 +441,23 @@ class pyResponseTDI:
                              "determine projections.")
         self.delayed_links_flat = self.delayed_links_flat.flatten()
         t_data = t0 + torch.arange(self.y_gw_length, dtype=torch.float64, device=dev) * self.dt
+        if self.tdi_chan not in ("XYZ", "AET", "AE"):
+            raise ValueError("tdi_chan must be 'XYZ', 'AET' or 'AE'.")
+        # lisatools' AET (response.py:659-673) in the TDI kernel's epilogue: the
+        # same values (zero outside the TDI range, as lisatools' AET of zeros)
+        rows = {"XYZ": 0, "AET": 3, "AE": 2}[self.tdi_chan]
+        aet = torch.zeros((rows, self.num_pts), dtype=torch.float64, device=dev) if rows else None
         with torch.cuda.device(dev), _lib.nvtx_range("flr.get_tdi_delays"):
             self.tdi_gen(self.delayed_links_flat, self.y_gw_flat, self.y_gw_length, self.num_pts,
                          t_data, self.unit_starts, self.unit_lengths, self.tdi_base_links,
                          self.tdi_link_combinations, self.tdi_signs, self.channels,
                          self.num_units, 3, self.order, self.sampling_frequency,
                          self.buffer_integer, self.A_in, self.deps, len(self.A_in), self.E_in,
-                         self.tdi_start_ind)
-        X, Y, Z = self.XYZ
-        if self.tdi_chan == "XYZ":
+                         self.tdi_start_ind, **({"aet": aet, "aet_rows": rows} if rows else {}))
+        if not rows:
+            X, Y, Z = self.XYZ
             return X, Y, Z
-        if self.tdi_chan in ("AET", "AE"):
-            # lisatools' AET (response.py:659-673) in one kernel: the same values
-            rows = 3 if self.tdi_chan == "AET" else 2
-            aet = torch.zeros((rows, self.num_pts), dtype=torch.float64, device=dev)
-            with torch.cuda.device(dev):
-                _lib.check(_lib.lib().flr_xyz_to_aet(
-                    self.delayed_links_flat.data_ptr(), aet.data_ptr(), self.num_pts,
-                    self.tdi_start_ind, rows, torch.cuda.current_stream(dev).cuda_stream))
-            return tuple(aet[r] for r in range(rows))
-        raise ValueError("tdi_chan must be 'XYZ', 'AET' or 'AE'.")
+        return tuple(aet[r] for r in range(rows))
 
     def status(self, reset: bool = False) -> int:
         """Kernel status bits of this instance's orbit handle (synchronises)."""

@@ -184,3 +184,29 @@ def test_batch_mixed_grouped_channels_and_sets(gpu_lib, chan):
             assert rel_l2(got[i][c], want[i][c]) <= MIXED_TOL
         if chan == "AE":
             assert not np.any(got[i][2])
+
+
+@pytest.mark.parametrize("orbit_kind", ["equal", "kepler"])
+def test_batch_mixed_bits_do_not_depend_on_the_tile(gpu_lib, orbit_kind):
+    """Every output sample of the mixed kernel is a function of its own
+    source and time alone: the per-item input scale is a power of two, the
+    differences are formed from the same samples, and the equal-delay
+    groups' tabulated weights equal the computed ones.  So tiles of 128, 512
+    and 1024 samples give the same bits."""
+    import fastlisaresponse_gb300 as flr
+
+    dt = 10.0
+    orb = flr.EqualArmlengthOrbits(t_max=2e6) if orbit_kind == "equal" else \
+        flr.KeplerianOrbits(t_max=2e6)
+    lengths = [3000, 41000, 123457, 9000]
+    hs, lam, beta, t0 = _sources(orb, dt, lengths, seed=61,
+                                 f=[3e-3, 1e-4, 2e-3, 8e-3])
+    outs = {}
+    for tile in (128, 512, 1024):
+        bat = flr.BatchedResponseTDI(1 / dt, tdi="2nd generation", orbits=orb, precision="mixed",
+                                     tile=tile)
+        outs[tile] = [_np(o) for o in bat(hs, lam, beta, t0=t0)]
+        assert bat.status() == 0
+    for tile in (128, 1024):
+        for a, b in zip(outs[tile], outs[512]):
+            assert np.array_equal(a, b), f"tile {tile}"

@@ -133,6 +133,25 @@ def test_chunked_device_call_matches_one_launch(gpu_lib, precision):
     assert bat.status() == 0
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_grouped_device_call_matches_one_launch(gpu_lib, precision):
+    """__call__(group_samples=g): runs of short sources share launches, long
+    ones are chunked, over two streams; same bits as one launch."""
+    import fastlisaresponse_gb300 as flr
+
+    dt = 10.0
+    orb = flr.EqualArmlengthOrbits(t_max=1.6e6)
+    lengths = [2300, 5000, 41000, 3000, 123457, 9000, 2500, 60001, 4100, 7000]
+    hs, lam, beta, t0 = _sources(orb, dt, lengths, seed=59)
+    bat = flr.BatchedResponseTDI(1 / dt, tdi="2nd generation", orbits=orb, precision=precision)
+    want = [_np(o) for o in bat(hs, lam, beta, t0=t0)]
+    for group in (10000, 50000, 10**9):
+        got = bat(hs, lam, beta, t0=t0, chunks=3, group_samples=group)
+        for g, w in zip(got, want):
+            assert np.array_equal(_np(g), w), f"group_samples={group}"
+    assert bat.status() == 0
+
+
 def test_output_range_rejects_bad_ranges(gpu_lib):
     import fastlisaresponse_gb300 as flr
 

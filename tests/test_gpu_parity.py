@@ -220,6 +220,36 @@ def test_response_wrapper_reference_test_setup(gpu_lib):
     assert abs(1.0 - flr.get_overlap(list(got), list(want))) < 1e-10
 
 
+@pytest.mark.parametrize("tdi_chan", ["AET", "AE"])
+def test_aet_epilogue_equals_separate_transform(gpu_lib, tdi_chan):
+    """A, E (, T) formed in the TDI kernel's epilogue (tdi_chan AET / AE)
+    equal flr_xyz_to_aet applied to the X, Y, Z of the same call, and the
+    X, Y, Z equal an XYZ instance's, bit for bit; 1st and 2nd generation."""
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+    from fastlisaresponse_gb300 import _lib
+
+    dt, n = 10.0, 30000
+    orb = flr.KeplerianOrbits(t_max=(n * dt // 1e4 + 3) * 1e4)
+    h = flr.gb_waveform(2e-22, 3e-3, 1e-15, 0.4, 1.1, 0.3, np.arange(n) * dt)
+    rows = 3 if tdi_chan == "AET" else 2
+    for gen in ("1st generation", "2nd generation"):
+        ref = flr.pyResponseTDI(1 / dt, n, tdi=gen, orbits=orb, tdi_chan="XYZ")
+        ref.get_projections(h, 0.8, -0.3)
+        xyz = torch.stack(list(ref.get_tdi_delays()))
+        resp = flr.pyResponseTDI(1 / dt, n, tdi=gen, orbits=orb, tdi_chan=tdi_chan)
+        resp.get_projections(h, 0.8, -0.3)
+        got = torch.stack(list(resp.get_tdi_delays()))
+        assert torch.equal(resp.XYZ, xyz), gen
+        want = torch.zeros((rows, n), dtype=torch.float64, device=xyz.device)
+        _lib.check(_lib.lib().flr_xyz_to_aet(xyz.data_ptr(), want.data_ptr(), n,
+                                             resp.tdi_start_ind, rows,
+                                             torch.cuda.current_stream().cuda_stream))
+        assert torch.equal(got, want), gen
+        assert resp.status() == 0
+
+
 def test_kernel_bounds_checks_flag_bad_windows(gpu_lib):
     """A start index of 0 makes the first samples' interpolation windows reach
     before the input; the kernel skips those reads, writes NaN there and sets
