@@ -74,7 +74,7 @@ SINGLE = dict(desc="one galactic binary (A 1e-22, f 2e-3 Hz, fdot 1e-14), 1 yr a
               A=1e-22, f=2e-3, fdot=1e-14)
 CPU_SLICE = 2**17         # output samples per CPU task (a slice of one source)
 SUBSET_STRIDE = 16        # plain FP64 leg: every 16th source by length (128 of 2048)
-E2E_GROUP_SAMPLES = 2**25  # samples per launch of the host pipeline
+E2E_GROUP_SAMPLES = 2**24  # samples per launch of the host pipeline
 SINGLE_CHUNKS = 8          # launches per 1 yr step (two streams: last waves overlap)
 SERVE_BATCH_SAMPLES = 2**23
 
@@ -835,6 +835,55 @@ def run_serving_section(args, device):
         out["rates"].append({"of_saturation": frac, "p50_ms": st["p50_ms"],
                              "p99_ms": st["p99_ms"],
                              "of_batched": st["throughput_samples_per_s"] / batched})
+
+    # the device-resident loop on the same request streams (outputs allocated
+    # before the clock starts; a poller records each request's completion)
+    samples = np.asarray([output_samples(nn) for nn in lengths], dtype=np.float64)
+
+    def run_device(rate):
+        outs = [torch.empty((3, int(nn)), dtype=torch.float64, device=device) for nn in lengths]
+        with flr.DeviceLoopServer(1 / dt, orbits=orb, capacity=count + 1, idle_seconds=0.02,
+                                  force_backend=device) as srv:
+            srv.submit(params[0], int(lengths[0]), int(sets[0])).result(timeout=60)  # warm-up
+            arrivals = (np.cumsum(rng.exponential(1.0 / rate, count)) if rate
+                        else np.zeros(count))
+            tickets = [None] * count
+
+            def client():
+                t_start = time.perf_counter()
+                for i in range(count):
+                    delay = t_start + arrivals[i] - time.perf_counter()
+                    if delay > 0:
+                        time.sleep(delay)
+                    tickets[i] = srv.submit(params[i], int(lengths[i]), int(sets[i]),
+                                            out=outs[i])
+
+            th = threading.Thread(target=client)
+            th.start()
+            pending = set(range(count))
+            while pending:
+                for i in [j for j in pending if tickets[j] is not None and tickets[j].done()]:
+                    pending.discard(i)
+                time.sleep(2e-5)
+            th.join()
+            assert srv.status() == 0
+            lat = np.asarray([t.latency for t in tickets]) * 1e3
+            span = max(t.t_done for t in tickets) - min(t.t_submit for t in tickets)
+            info = srv.info()
+        del outs
+        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "throughput_samples_per_s": float(samples.sum() / span),
+                "launches": int(info["launches"])}
+
+    dsat = run_device(None)
+    dl = {"saturation_samples_per_s": dsat["throughput_samples_per_s"], "rates": []}
+    for frac in (0.5, 0.8, 0.9):
+        st = run_device(frac * cap)
+        dl["rates"].append({"of_response_server_saturation": frac, "p50_ms": st["p50_ms"],
+                            "p99_ms": st["p99_ms"], "launches": st["launches"],
+                            "of_batched": st["throughput_samples_per_s"] / batched})
+    out["device_loop"] = dl
+    full["device_loop"] = dl
     return out, full
 
 

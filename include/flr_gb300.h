@@ -82,6 +82,13 @@ const char *flr_version(void);
 /* Text of the last error raised on the calling thread ("" if none). */
 const char *flr_last_error(void);
 
+/* Page-locked host memory of exactly `bytes` bytes (cudaHostAlloc, portable
+ * to every device), for the host buffers of asynchronous copies (no
+ * reference counterpart; the Python HostArray uses it).  flr_host_free
+ * releases it. */
+int flr_host_alloc(size_t bytes, void **out);
+int flr_host_free(void *ptr);
+
 /*
  * Upload orbit tables and return a handle (replaces OrbitsWrap*_responselisa,
  * binding_flr.hpp:35-59).  Layout as lisaanalysistools' pycppdetector_args:
@@ -412,6 +419,38 @@ int flr_get_response_noalloc(double orbit_dt, int orbit_N, const double *ltt_arr
  */
 int flr_noalloc_status(uint32_t *bits, int reset, void *stream);
 
+
+/*
+ * ------------------------------------------------------------------------
+ * Device-resident serving (no reference counterpart).  A server holds a list
+ * of up to `capacity` sources in page-locked host memory mapped into the
+ * device; flr_server_submit appends one source (its descriptor, waveform
+ * parameters and tile count) and publishes its tiles, and a persistent launch
+ * of the plan's mixed fused kernel (flr_server_pump) claims published tiles
+ * as they arrive, so requests submitted while it runs need no new launch.
+ * The block that writes a source's last tile sets its done flag (host
+ * memory, flr_server_done_flags; read with acquire loads).  The launch
+ * leaves after `idle_seconds` without claimable work or once flr_server_stop
+ * is called (after the work already published); flr_server_pump relaunches
+ * it when sources are not done and none is running.  Every wait of the
+ * kernel is bounded (the idle time and a poll count).  Sources are whole
+ * (no out_begin/out_end, diagnostics or inner products); h NULL with
+ * waveform parameters generates the waveform inside the kernel.  Results are
+ * those of flr_batch_run_gb / flr_batch_run on the same sources.  Not
+ * thread-safe: one host thread submits and pumps.
+ */
+typedef struct flr_server flr_server;
+int flr_server_create(flr_batch_plan *plan, int capacity, int chan, double idle_seconds,
+                      flr_server **out);
+int flr_server_submit(flr_server *server, const flr_batch_source *source,
+                      const flr_gb_params *params, int *slot);
+int flr_server_pump(flr_server *server, void *stream);
+/* info[0..4] = sources submitted, tiles published, lowest source not known
+ * to be done, launches so far, 1 while a launch may be running. */
+int flr_server_info(const flr_server *server, long long *info, int n_info);
+const unsigned *flr_server_done_flags(const flr_server *server);
+int flr_server_stop(flr_server *server);
+int flr_server_destroy(flr_server *server);
 
 #ifdef __cplusplus
 }

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -50,6 +51,32 @@ struct flr_batch_plan {
     double *d_partial;         // per-tile partial inner products (runs that ask for them)
     size_t cap_partial;
     bool done_pending;
+};
+
+// Device-resident serving: a source list in page-locked host memory mapped
+// into the device, appended to by the host while a persistent launch of the
+// fused kernel's serving instance claims its tiles (flr_fused_kernel.cuh).
+struct flr_server {
+    flr_batch_plan *plan = nullptr;
+    int chan = 0;
+    bool d2 = false;
+    int cap = 0;
+    long long idle_ns = 0;
+    unsigned char *h_block = nullptr;        // the mapped block
+    flr::FusedSource *h_src = nullptr, *d_src = nullptr;
+    flr::GbParams *h_gb = nullptr, *d_gb = nullptr;
+    long long *h_tile_start = nullptr, *d_tile_start = nullptr;  // cap + 1
+    unsigned long long *h_published = nullptr, *d_published = nullptr;
+    int *h_stop = nullptr, *d_stop = nullptr;
+    unsigned *h_done = nullptr, *d_done = nullptr;
+    unsigned long long *d_next = nullptr;   // claim counter (device)
+    unsigned *d_tiles_done = nullptr;       // per source (device)
+    int count = 0;                          // sources submitted
+    long long items = 0;                    // tiles published
+    int first_open = 0;                     // lowest source not known to be done
+    long long launches = 0;
+    cudaEvent_t ran = nullptr;              // recorded after the last launch
+    bool launched = false;
 };
 
 struct flr_batch_graph {
@@ -898,6 +925,179 @@ int flr_batch_graph_destroy(flr_batch_graph *g) {
     for (int b = 0; b < 2; ++b)
         if (g->pending[b]) cudaEventSynchronize(g->done[b]);
     release_graph(g);
+    return FLR_OK;
+}
+
+
+// ------------------------------------------------------------------ serving --
+
+int flr_server_create(flr_batch_plan *plan, int capacity, int chan, double idle_seconds,
+                      flr_server **out) {
+    flr::set_last_error("");
+    if (!plan || !out) return fail(FLR_E_INVALID_ARGUMENT, "plan and out must not be NULL");
+    *out = nullptr;
+    if (!plan->mixed) return fail(FLR_E_INVALID_ARGUMENT, "serving needs a mixed-precision plan");
+    if (capacity < 1 || capacity > (1 << 24))
+        return fail(FLR_E_INVALID_ARGUMENT, "capacity must be in [1, 2^24]");
+    if (chan != FLR_CHAN_XYZ && chan != FLR_CHAN_AET && chan != FLR_CHAN_AE)
+        return fail(FLR_E_INVALID_ARGUMENT, "chan must be FLR_CHAN_XYZ, _AET or _AE");
+    if (!(idle_seconds > 0.0) || idle_seconds > 60.0)
+        return fail(FLR_E_INVALID_ARGUMENT, "idle_seconds must be in (0, 60]");
+    int rc = current_device_is(plan->device);
+    if (rc) return rc;
+    flr_server *sv = new flr_server();
+    sv->plan = plan;
+    sv->chan = chan;
+    sv->d2 = plan->base.d2 && chan == FLR_CHAN_XYZ;
+    sv->cap = capacity;
+    sv->idle_ns = (long long)(idle_seconds * 1e9);
+    auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t o_src = 0;
+    const size_t o_gb = up(o_src + sizeof(flr::FusedSource) * (size_t)capacity);
+    const size_t o_ts = up(o_gb + sizeof(flr::GbParams) * (size_t)capacity);
+    const size_t o_pub = up(o_ts + sizeof(long long) * ((size_t)capacity + 1));
+    const size_t o_stop = o_pub + 64;
+    const size_t o_done = up(o_stop + 64);
+    const size_t bytes = up(o_done + sizeof(unsigned) * (size_t)capacity);
+    void *hb = nullptr, *db = nullptr;
+    cudaError_t err = cudaHostAlloc(&hb, bytes, cudaHostAllocMapped | cudaHostAllocPortable);
+    if (err == cudaSuccess) err = cudaHostGetDevicePointer(&db, hb, 0);
+    if (err == cudaSuccess) err = cudaMalloc(&sv->d_next, sizeof(unsigned long long));
+    if (err == cudaSuccess) err = cudaMalloc(&sv->d_tiles_done, sizeof(unsigned) * (size_t)capacity);
+    if (err == cudaSuccess) err = cudaMemset(sv->d_next, 0, sizeof(unsigned long long));
+    if (err == cudaSuccess) err = cudaMemset(sv->d_tiles_done, 0, sizeof(unsigned) * (size_t)capacity);
+    if (err == cudaSuccess) err = cudaEventCreateWithFlags(&sv->ran, cudaEventDisableTiming);
+    sv->h_block = static_cast<unsigned char *>(hb);
+    if (err != cudaSuccess) {
+        flr_server_destroy(sv);
+        return cuda_fail(err, "allocating the serving buffers");
+    }
+    unsigned char *h = sv->h_block, *d = static_cast<unsigned char *>(db);
+    std::memset(h, 0, bytes);
+    sv->h_src = reinterpret_cast<flr::FusedSource *>(h + o_src);
+    sv->h_gb = reinterpret_cast<flr::GbParams *>(h + o_gb);
+    sv->h_tile_start = reinterpret_cast<long long *>(h + o_ts);
+    sv->h_published = reinterpret_cast<unsigned long long *>(h + o_pub);
+    sv->h_stop = reinterpret_cast<int *>(h + o_stop);
+    sv->h_done = reinterpret_cast<unsigned *>(h + o_done);
+    sv->d_src = reinterpret_cast<flr::FusedSource *>(d + o_src);
+    sv->d_gb = reinterpret_cast<flr::GbParams *>(d + o_gb);
+    sv->d_tile_start = reinterpret_cast<long long *>(d + o_ts);
+    sv->d_published = reinterpret_cast<unsigned long long *>(d + o_pub);
+    sv->d_stop = reinterpret_cast<int *>(d + o_stop);
+    sv->d_done = reinterpret_cast<unsigned *>(d + o_done);
+    for (int i = 1; i <= capacity; ++i) sv->h_tile_start[i] = INT64_MAX;  // not yet published
+    *out = sv;
+    return FLR_OK;
+}
+
+int flr_server_submit(flr_server *sv, const flr_batch_source *source, const flr_gb_params *params,
+                      int *slot) {
+    flr::set_last_error("");
+    if (!sv || !source || !slot) return fail(FLR_E_INVALID_ARGUMENT, "NULL argument");
+    if (sv->count >= sv->cap)
+        return fail(FLR_E_INVALID_ARGUMENT, "the server's source list is full");
+    if (source->y_out || source->d_rec_out || source->d_em_out || source->d_tdi_out ||
+        source->data || source->inner || source->out_end > source->out_begin)
+        return fail(FLR_E_INVALID_ARGUMENT,
+                    "serving takes whole sources without diagnostics or inner products");
+    if (!source->out) return fail(FLR_E_INVALID_ARGUMENT, "out must not be NULL");
+    // the batch path's checks and descriptor, for one source
+    const StageLayout lay = stage_layout(1, params != nullptr);
+    std::vector<unsigned char> stage(lay.bytes);
+    bool diag = false, inner = false;
+    long tiles = 0;
+    int rc = fill_stage(sv->plan, source, 1, params, 1, lay, stage.data(), &diag, &inner, &tiles);
+    if (rc) return rc;
+    const int i = sv->count;
+    std::memcpy(sv->h_src + i, stage.data(), sizeof(flr::FusedSource));
+    if (params)
+        std::memcpy(sv->h_gb + i, stage.data() + lay.gb, sizeof(flr::GbParams));
+    else
+        std::memset(sv->h_gb + i, 0, sizeof(flr::GbParams));
+    sv->h_done[i] = 0u;
+    const long long end = sv->items + tiles;
+    sv->h_tile_start[i + 1] = end;
+    // publish: the descriptor and prefix sum are visible before the count
+    __atomic_store_n(sv->h_published, (unsigned long long)end, __ATOMIC_RELEASE);
+    sv->items = end;
+    sv->count = i + 1;
+    *slot = i;
+    return FLR_OK;
+}
+
+int flr_server_pump(flr_server *sv, void *stream) {
+    flr::set_last_error("");
+    if (!sv) return fail(FLR_E_INVALID_ARGUMENT, "server must not be NULL");
+    int rc = current_device_is(sv->plan->device);
+    if (rc) return rc;
+    if (sv->launched) {
+        const cudaError_t q = cudaEventQuery(sv->ran);
+        if (q == cudaErrorNotReady) return FLR_OK;  // still running: it will claim new items
+        if (q != cudaSuccess) return cuda_fail(q, "querying the serving kernel");
+        sv->launched = false;
+    }
+    while (sv->first_open < sv->count &&
+           __atomic_load_n(sv->h_done + sv->first_open, __ATOMIC_ACQUIRE) != 0u)
+        ++sv->first_open;
+    if (sv->first_open >= sv->count || __atomic_load_n(sv->h_stop, __ATOMIC_RELAXED)) return FLR_OK;
+    flr::FusedArgs a = sv->plan->base;
+    a.sources = sv->d_src;
+    a.tile_start = reinterpret_cast<const long *>(sv->d_tile_start);
+    a.tile_base = reinterpret_cast<const long *>(sv->d_tile_start);
+    a.gb = sv->d_gb;
+    a.num_sources = sv->cap;
+    a.chan = sv->chan;
+    a.partial = nullptr;
+    a.work_next = sv->d_next;
+    a.srv_published = sv->d_published;
+    a.srv_stop = sv->d_stop;
+    a.srv_tiles_done = sv->d_tiles_done;
+    a.srv_done = sv->d_done;
+    a.srv_idle_ns = sv->idle_ns;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t err = flr::launch_fused_server(sv->plan->grouped, sv->d2, a, sv->plan->grid_max,
+                                               sv->plan->smem, st);
+    if (err == cudaSuccess) err = cudaEventRecord(sv->ran, st);
+    if (err != cudaSuccess) return cuda_fail(err, "launching the serving kernel");
+    sv->launched = true;
+    ++sv->launches;
+    return FLR_OK;
+}
+
+int flr_server_info(const flr_server *sv, long long *info, int n_info) {
+    if (!sv || !info) return fail(FLR_E_INVALID_ARGUMENT, "NULL argument");
+    const long long vals[] = {sv->count, sv->items, sv->first_open, sv->launches,
+                              sv->launched ? 1LL : 0LL};
+    for (int i = 0; i < n_info && i < 5; ++i) info[i] = vals[i];
+    return FLR_OK;
+}
+
+const unsigned *flr_server_done_flags(const flr_server *sv) { return sv ? sv->h_done : nullptr; }
+
+int flr_server_stop(flr_server *sv) {
+    flr::set_last_error("");
+    if (!sv) return fail(FLR_E_INVALID_ARGUMENT, "server must not be NULL");
+    __atomic_store_n(sv->h_stop, 1, __ATOMIC_RELEASE);
+    if (sv->launched) {
+        const cudaError_t err = cudaEventSynchronize(sv->ran);
+        sv->launched = false;
+        if (err != cudaSuccess) return cuda_fail(err, "waiting for the serving kernel");
+    }
+    return FLR_OK;
+}
+
+int flr_server_destroy(flr_server *sv) {
+    if (!sv) return FLR_OK;
+    if (sv->h_block) {
+        __atomic_store_n(sv->h_stop, 1, __ATOMIC_RELEASE);
+        if (sv->launched) cudaEventSynchronize(sv->ran);
+    }
+    if (sv->ran) cudaEventDestroy(sv->ran);
+    if (sv->d_next) cudaFree(sv->d_next);
+    if (sv->d_tiles_done) cudaFree(sv->d_tiles_done);
+    if (sv->h_block) cudaFreeHost(sv->h_block);
+    delete sv;
     return FLR_OK;
 }
 

@@ -86,6 +86,27 @@ extern "C" {
 
 const char *flr_version(void) { return "flr_gb300 0.1.0 sm_103a"; }
 
+int flr_host_alloc(size_t bytes, void **out) {
+    g_last_error.clear();
+    if (!out) return fail(FLR_E_INVALID_ARGUMENT, "out must not be NULL");
+    *out = nullptr;
+    if (bytes == 0) return fail(FLR_E_INVALID_ARGUMENT, "bytes must be positive");
+    cudaError_t err = cudaHostAlloc(out, bytes, cudaHostAllocPortable);
+    if (err != cudaSuccess) {
+        *out = nullptr;
+        return cuda_fail(err, "allocating page-locked host memory");
+    }
+    return FLR_OK;
+}
+
+int flr_host_free(void *ptr) {
+    g_last_error.clear();
+    if (!ptr) return FLR_OK;
+    cudaError_t err = cudaFreeHost(ptr);
+    if (err != cudaSuccess) return cuda_fail(err, "releasing page-locked host memory");
+    return FLR_OK;
+}
+
 const char *flr_last_error(void) { return g_last_error.c_str(); }
 
 int flr_orbits_create(double dt, int N, const double *n_arr, const double *ltt_arr,

@@ -61,6 +61,16 @@ cudaError_t launch_fused(bool mixed, bool grouped, bool diag, bool inner, bool d
                             dim3(kThreads), args, smem_bytes, stream);
 }
 
+cudaError_t launch_fused_server(bool grouped, bool d2, const FusedArgs &a, int grid,
+                                size_t smem_bytes, cudaStream_t stream) {
+    const void *fn = fused_fn_server(grouped, d2);
+    cudaError_t err =
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    if (err != cudaSuccess) return err;
+    void *args[] = {const_cast<FusedArgs *>(&a)};
+    return cudaLaunchKernel(fn, dim3(grid), dim3(kThreads), args, smem_bytes, stream);
+}
+
 cudaError_t launch_inner_reduce(const FusedArgs &a, cudaStream_t stream) {
     if (a.num_sources <= 0) return cudaSuccess;
     const long threads = 6L * a.num_sources;

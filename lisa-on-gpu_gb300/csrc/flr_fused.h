@@ -20,6 +20,9 @@ constexpr long kFusedWaitPolls = 1L << 20;
 // alternatives are in the plan report's documentation).
 constexpr int kFusedThreads = 256;
 constexpr int kFusedStagingDepth = 1;
+// Bound of a serving block's polls for new work (each ~1 us of sleep), on top
+// of the idle time: a block leaves after at most this many.
+constexpr long kServerMaxPolls = 1L << 22;
 // Status bits of the fused kernel (beside those of flr_device.cuh):
 constexpr unsigned kStatusStaging = 0x10u;      // an item's copy missed its first wait:
                                                 // that item's outputs are NaN
@@ -110,6 +113,18 @@ struct FusedArgs {
     // counter's old value.  A block that runs faster takes more items, so no
     // SM idles while others finish.  NULL: static striding by gridDim.x.
     unsigned long long *work_next;
+    // Device-resident serving (the server instances): sources, tile_start and
+    // the waveform parameters are in page-locked host memory mapped into the
+    // device and grow while the kernel runs; tile_start entries not yet
+    // published hold INT64_MAX.  Blocks claim items below srv_published (a
+    // CAS on work_next, which persists across launches), and leave after
+    // srv_idle_ns without claimable work or once srv_stop is set with none
+    // left.  The block that finishes a source's last tile sets srv_done.
+    const unsigned long long *srv_published;  // work items published (mapped)
+    const int *srv_stop;                      // mapped
+    unsigned int *srv_tiles_done;             // per source, device memory
+    unsigned int *srv_done;                   // per source, mapped
+    long long srv_idle_ns;
     int num_sources;
     // per work item: the six partial inner products of its tile (inner-product
     // runs only; reduced per source by launch_inner_reduce)
@@ -180,5 +195,11 @@ cudaError_t launch_fused(bool mixed, bool grouped, bool diag, bool inner, bool d
                          const FusedArgs &a, int grid, size_t smem_bytes, cudaStream_t stream);
 // The difference-form mixed instances (flr_fused_d2.cu).
 const void *fused_fn_d2(bool grouped, bool diag, bool inner);
+// Serving instances (mixed; d2: difference forms for XYZ outputs): a launch
+// that claims published items until it is idle or stopped.  Sets the
+// instance's shared-memory limit before launching.
+const void *fused_fn_server(bool grouped, bool d2);
+cudaError_t launch_fused_server(bool grouped, bool d2, const FusedArgs &a, int grid,
+                                size_t smem_bytes, cudaStream_t stream);
 
 }  // namespace flr

@@ -118,7 +118,7 @@ __host__ __device__ constexpr size_t align128(size_t x) { return (x + 127) & ~si
 
 __host__ __device__ inline Layout layout(bool mixed, int win_max, int y_max) {
     Layout L{};
-    size_t off = 384;  // mbarrier, scale, warp maxima, segment cache, window ends
+    size_t off = 640;  // mbarrier, scale, warp maxima, segment cache, window ends, source copy
     L.set = off;
     off = align128(off + sizeof(FusedTdiSet));
     L.edf = off;
@@ -1088,9 +1088,83 @@ __device__ __forceinline__ bool mixed_interp_any(const FusedArgs &a, const float
 // compiler's choice (a minimum of 0 blocks leaves it unspecified).
 // kInner: the instance that forms per-tile inner products with FusedSource
 // data (FusedArgs::partial) and writes the channels only where out is set.
-template <bool kMixed, bool kDiag, bool kGrouped, bool kInner, bool kD2>
+// ------------------------------------------------ device-resident serving ----
+//
+// The server instances run the same item code over a source list that the
+// host appends to in mapped page-locked memory while the kernel runs.  Such
+// memory is read with ld.relaxed/acquire.sys, never through the read-only
+// cache, so a line cached before the host wrote it is not reused.
+
+__device__ __forceinline__ unsigned long long ld_acquire_sys(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ long long ld_relaxed_sys(const long long *p) {
+    long long v;
+    asm volatile("ld.relaxed.sys.global.s64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Called by every thread of a block between items.  Thread 0 first reports
+// the finished item (`done_source` >= 0: its source, with `done_tiles` tiles
+// in all) -- every thread has fenced its outputs at system scope before the
+// barrier, so the flag the last tile sets is seen after them -- then claims
+// the next published item with a CAS on the counter, polling (bounded by
+// kServerMaxPolls and srv_idle_ns) while none is published.  Returns the item,
+// or -1: the block leaves.
+__device__ long long server_next_item(const FusedArgs &a, long long *slot, int tid,
+                                      int done_source, long long done_tiles) {
+    __threadfence_system();
+    __syncthreads();
+    if (tid == 0) {
+        if (done_source >= 0) {
+            const unsigned old = atomicAdd(a.srv_tiles_done + done_source, 1u);
+            if ((long long)old + 1 == done_tiles) {
+                __threadfence_system();
+                asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(a.srv_done + done_source),
+                             "r"(1u)
+                             : "memory");
+            }
+        }
+        long long got = -1;
+        const unsigned long long t_start = globaltimer_ns();
+        for (long it = 0; it < kServerMaxPolls; ++it) {
+            const unsigned long long pub = ld_acquire_sys(a.srv_published);
+            unsigned long long c = atomicAdd(a.work_next, 0ull);
+            while (c < pub) {
+                const unsigned long long prev = atomicCAS(a.work_next, c, c + 1ull);
+                if (prev == c) {
+                    got = (long long)c;
+                    break;
+                }
+                c = prev;
+            }
+            if (got >= 0) break;
+            int stop;
+            asm volatile("ld.relaxed.sys.global.s32 %0, [%1];" : "=r"(stop) : "l"(a.srv_stop) : "memory");
+            if (stop != 0 || globaltimer_ns() - t_start > (unsigned long long)a.srv_idle_ns) break;
+            __nanosleep(1000);
+        }
+        *slot = got;
+    }
+    __syncthreads();
+    const long long w = *slot;
+    __syncthreads();
+    return w;
+}
+
+template <bool kMixed, bool kDiag, bool kGrouped, bool kInner, bool kD2, bool kServer = false>
 __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
     fused_kernel(const FusedArgs a) {
+    static_assert(!kServer || (kMixed && !kDiag && !kInner), "serving runs the plain mixed instances");
     static_assert(kMixed || !kD2, "the difference forms are mixed-arithmetic forms");
     static_assert(kMixed || !kGrouped, "the grouped form is a mixed-arithmetic form");
     static_assert(!(kDiag && kInner), "diagnostics and inner products are separate instances");
@@ -1103,6 +1177,14 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
     double *warp_max = reinterpret_cast<double *>(smem + 64);
     int2 *ends_sm = reinterpret_cast<int2 *>(smem + 256);  // (min d, max d) per link end
     long long *next_sm = reinterpret_cast<long long *>(smem + 352);  // next item, 2 slots
+    // serving: the item's source descriptor and waveform parameters, copied
+    // from mapped memory
+    FusedSource *src_sm = reinterpret_cast<FusedSource *>(smem + 384);
+    GbParams *gb_sm = reinterpret_cast<GbParams *>(smem + 576);
+    static_assert(sizeof(FusedSource) <= 192 && sizeof(GbParams) <= 64, "header layout");
+    static_assert(sizeof(FusedSource) % 8 == 0 && sizeof(FusedSource) / 8 <= 32 &&
+                      sizeof(GbParams) % 8 == 0,
+                  "descriptor copies: whole 8-byte words, one per thread of a warp");
     static_assert(kThreads / 32 <= 8, "warp maxima: 8 slots");
     static_assert(sizeof(SegCache) <= 128, "segment cache: 128 bytes");
     FusedTdiSet *set = reinterpret_cast<FusedTdiSet *>(smem + lay.set);
@@ -1130,29 +1212,74 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
     // read by all after the item's last barrier (the loop increment; a
     // `continue` passes through it too); the two slots alternate, so a slot
     // is rewritten only after every thread has read it.
-    for (long wi = blockIdx.x; wi < num_work; wi = next_sm[par], par ^= 1) {
-        if (tid == 0)
+    // serving: the finished item's source and tile count, for its report
+    int srv_src = -1;
+    long long srv_tiles = 0;
+    long wi0 = blockIdx.x;
+    if (kServer) wi0 = (long)server_next_item(a, next_sm, tid, -1, 0);
+    for (long wi = wi0; kServer ? wi >= 0 : wi < num_work;
+         wi = kServer ? (long)server_next_item(a, next_sm + 1, tid, srv_src, srv_tiles)
+                      : (long)next_sm[par],
+              par ^= 1) {
+        if (!kServer && tid == 0)
             next_sm[par] = a.work_next ? (long long)gridDim.x + (long long)atomicAdd(a.work_next, 1ull)
                                        : wi + gridDim.x;
         // source of item wi: the last s with tile_start[s] <= wi.  A block's
         // items only grow and mostly stay in one source, so the current
         // source is checked first; otherwise a binary search from the next.
-        if (__ldg(a.tile_start + si + 1) <= wi) {
-            ++si;
-            int hi = a.num_sources - 1;
-            while (si < hi) {
-                const int mid = (si + hi + 1) >> 1;
-                if (__ldg(a.tile_start + mid) <= wi)
-                    si = mid;
-                else
-                    hi = mid - 1;
+        long tile_idx;
+        if (kServer) {
+            // claimed items grow and their sources are published (entries not
+            // yet published read as INT64_MAX): gallop up from the last source,
+            // then bisect
+            const long long *ts_m = reinterpret_cast<const long long *>(a.tile_start);
+            if (ld_relaxed_sys(ts_m + si + 1) <= wi) {
+                int lo = si + 1, step = 1;
+                while (lo + step < a.num_sources && ld_relaxed_sys(ts_m + lo + step) <= wi) {
+                    lo += step;
+                    step *= 2;
+                }
+                int hi = min(lo + step, a.num_sources) - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (ld_relaxed_sys(ts_m + mid) <= wi)
+                        lo = mid;
+                    else
+                        hi = mid - 1;
+                }
+                si = lo;
             }
+            const long long first = ld_relaxed_sys(ts_m + si);
+            srv_src = si;
+            srv_tiles = ld_relaxed_sys(ts_m + si + 1) - first;
+            tile_idx = wi - first;
+            // the descriptor and parameters into shared memory
+            const long long *from = reinterpret_cast<const long long *>(a.sources + si);
+            if (tid < (int)(sizeof(FusedSource) / 8))
+                reinterpret_cast<long long *>(src_sm)[tid] = ld_relaxed_sys(from + tid);
+            const long long *gfrom = reinterpret_cast<const long long *>(a.gb + si);
+            if (tid >= 32 && tid < 32 + (int)(sizeof(GbParams) / 8))
+                reinterpret_cast<long long *>(gb_sm)[tid - 32] = ld_relaxed_sys(gfrom + tid - 32);
+            __syncthreads();
+        } else {
+            if (__ldg(a.tile_start + si + 1) <= wi) {
+                ++si;
+                int hi = a.num_sources - 1;
+                while (si < hi) {
+                    const int mid = (si + hi + 1) >> 1;
+                    if (__ldg(a.tile_start + mid) <= wi)
+                        si = mid;
+                    else
+                        hi = mid - 1;
+                }
+            }
+            tile_idx = wi - __ldg(a.tile_base + si);
         }
-        const long tile_idx = wi - __ldg(a.tile_base + si);
-        const FusedSource &src = a.sources[si];
+        const FusedSource &src = kServer ? *src_sm : a.sources[si];
+        const GbParams *gbp = kServer ? gb_sm : (a.gb ? a.gb + si : nullptr);
         // the input outside the staged window: the stored waveform, or the
         // source's generator when it has none
-        const HSrc hsrc{src.h, a.gb ? a.gb + si : nullptr, src.t0, a.dt};
+        const HSrc hsrc{src.h, gbp, src.t0, a.dt};
         const long n = src.n;
         const int ps = src.ps, ts = src.ts;
         const double t0 = src.t0;
@@ -1240,7 +1367,7 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
         // 2. stage the window: generated in place for a source without a stored
         // waveform, else one bulk copy
         if (W > 0 && src.h == nullptr) {
-            const GbCoefs gc = gb_coefs(a.gb[si]);
+            const GbCoefs gc = gb_coefs(*gbp);
             for (int i = tid; i < W; i += kThreads)
                 hraw[i] = gb_sample(gc, t0 + (double)(wlo + i) * a.dt);
             __syncthreads();

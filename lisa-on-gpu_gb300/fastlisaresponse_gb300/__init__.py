@@ -13,6 +13,7 @@ from .batch import BatchedResponseTDI, BatchGraph
 from .binding import LISAResponseWrap, LISAResponseWrapGPU, OrbitsWrap, OrbitsWrapGPU_responselisa
 from .orbits import EqualArmlengthOrbits, KeplerianOrbits, Orbits, read_lisa_orbits
 from .serve import Request, ResponseServer
+from .serve_device import DeviceLoopServer, DeviceTicket
 from .response import (ResponseWrapper, lagrange_tables, pyResponseTDI, sky_basis,
                        tdi_unit_tables)
 from .utils import AET, HostArray, get_overlap
@@ -21,7 +22,7 @@ from .waveforms import GBWave, gb_waveform, time_grid
 __version__ = "0.1.0"
 
 __all__ = [
-    "AET", "BatchGraph", "HostArray", "BatchedResponseTDI", "EqualArmlengthOrbits", "FLRError", "GBWave", "KeplerianOrbits",
+    "AET", "BatchGraph", "DeviceLoopServer", "DeviceTicket", "HostArray", "BatchedResponseTDI", "EqualArmlengthOrbits", "FLRError", "GBWave", "KeplerianOrbits",
     "LISAResponseWrap", "LISAResponseWrapGPU", "Orbits", "OrbitsWrap",
     "OrbitsWrapGPU_responselisa", "ResponseWrapper", "autotune", "build", "describe_status",
     "gb_waveform", "get_overlap", "lagrange_tables", "library_path", "needs_build",

@@ -35,6 +35,7 @@ SOURCES = {
     "flr_noalloc.cu": ["--fmad=false"],
     "flr_fused.cu": ["--fmad=false"],
     "flr_fused_d2.cu": ["--fmad=false"],
+    "flr_fused_server.cu": ["--fmad=false"],
     "flr_batch.cu": [],
     "flr_waveform.cu": ["--fmad=false"],
 }

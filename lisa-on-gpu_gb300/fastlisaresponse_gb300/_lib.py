@@ -40,6 +40,8 @@ _p = ctypes.c_void_p
 
 _SIGNATURES = {
     "flr_version": (ctypes.c_char_p, []),
+    "flr_host_alloc": (_i, [ctypes.c_size_t, ctypes.POINTER(_p)]),
+    "flr_host_free": (_i, [_p]),
     "flr_last_error": (ctypes.c_char_p, []),
     "flr_orbits_create": (_i, [_d, _i, _p, _p, _p, _p, _p, _p, _d, ctypes.POINTER(_p)]),
     "flr_orbits_destroy": (_i, [_p]),

@@ -4,8 +4,9 @@ host-device copies."""
 
 from __future__ import annotations
 
+import ctypes
 import math
-import mmap
+import weakref
 
 import numpy as np
 
@@ -71,35 +72,36 @@ def get_overlap(sig1, sig2, phase_maximize=False, use_gpu=False):
 
 
 class HostArray:
-    """A NumPy array in page-locked host memory, made by page-locking an
-    anonymous memory map in place (cudaHostRegister): copies between it and
-    the GPU run asynchronously (``BatchedResponseTDI.run_host``).  The map is
-    page-aligned and its own, so registrations never share a page, and its
-    size is exact (no power-of-two rounding of a caching allocator).  Call
-    :meth:`release` (or use it as a context manager) to unlock it.
+    """A NumPy array in page-locked host memory of exactly its size
+    (cudaHostAlloc through ``flr_host_alloc``; a caching allocator would round
+    it up to a power of two): copies between it and the GPU run
+    asynchronously on the copy engines (``BatchedResponseTDI.run_host``).
+    The memory is freed when the last view of it (``.array``, ``.tensor`` or
+    anything made from them) is gone; :meth:`release` (or leaving a ``with``
+    block) drops this object's own references.
 
     ``HostArray(shape, dtype).array`` is the NumPy view;
     ``.tensor`` a CPU torch tensor on the same memory."""
 
     def __init__(self, shape, dtype=np.float64):
+        from . import _lib
+
         self.shape = tuple(np.atleast_1d(shape).tolist())
         self.dtype = np.dtype(dtype)
-        nbytes = int(np.prod(self.shape)) * self.dtype.itemsize
-        self._map = mmap.mmap(-1, max(nbytes, 1))
-        self.array = np.frombuffer(self._map, dtype=self.dtype,
-                                   count=int(np.prod(self.shape))).reshape(self.shape)
-        self._registered = False
-        if nbytes:
-            rc = int(torch.cuda.cudart().cudaHostRegister(self.array.ctypes.data, nbytes, 0))
-            if rc != 0:
-                raise RuntimeError(f"cudaHostRegister failed ({rc})")
-            self._registered = True
+        count = int(np.prod(self.shape))
+        nbytes = count * self.dtype.itemsize
+        lib = _lib.lib()
+        ptr = ctypes.c_void_p()
+        _lib.check(lib.flr_host_alloc(max(nbytes, 1), ctypes.byref(ptr)))
+        raw = (ctypes.c_char * max(nbytes, 1)).from_address(ptr.value)
+        # freed with the ctypes block, which every NumPy/torch view keeps alive
+        weakref.finalize(raw, lib.flr_host_free, ptr.value)
+        self.array = np.frombuffer(raw, dtype=self.dtype, count=count).reshape(self.shape)
         self.tensor = torch.from_numpy(self.array)
 
     def release(self):
-        if self._registered:
-            torch.cuda.cudart().cudaHostUnregister(self.array.ctypes.data)
-            self._registered = False
+        self.array = None
+        self.tensor = None
 
     def __enter__(self):
         return self
@@ -107,9 +109,3 @@ class HostArray:
     def __exit__(self, *exc):
         self.release()
         return False
-
-    def __del__(self):
-        try:
-            self.release()
-        except Exception:
-            pass
