@@ -447,7 +447,7 @@ int flr_server_submit(flr_server *server, const flr_batch_source *source,
 int flr_server_pump(flr_server *server, void *stream);
 /* info[0..4] = sources submitted, tiles published, lowest source not known
  * to be done, launches so far, 1 while a launch may be running. */
-int flr_server_info(const flr_server *server, long long *info, int n_info);
+int flr_server_info(flr_server *server, long long *info, int n_info);
 const unsigned *flr_server_done_flags(const flr_server *server);
 int flr_server_stop(flr_server *server);
 int flr_server_destroy(flr_server *server);

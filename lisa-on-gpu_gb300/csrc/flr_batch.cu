@@ -1026,20 +1026,25 @@ int flr_server_submit(flr_server *sv, const flr_batch_source *source, const flr_
     return FLR_OK;
 }
 
+static void advance_first_open(flr_server *sv) {
+    while (sv->first_open < sv->count &&
+           __atomic_load_n(sv->h_done + sv->first_open, __ATOMIC_ACQUIRE) != 0u)
+        ++sv->first_open;
+}
+
 int flr_server_pump(flr_server *sv, void *stream) {
     flr::set_last_error("");
     if (!sv) return fail(FLR_E_INVALID_ARGUMENT, "server must not be NULL");
     int rc = current_device_is(sv->plan->device);
     if (rc) return rc;
+    advance_first_open(sv);
     if (sv->launched) {
         const cudaError_t q = cudaEventQuery(sv->ran);
         if (q == cudaErrorNotReady) return FLR_OK;  // still running: it will claim new items
         if (q != cudaSuccess) return cuda_fail(q, "querying the serving kernel");
         sv->launched = false;
     }
-    while (sv->first_open < sv->count &&
-           __atomic_load_n(sv->h_done + sv->first_open, __ATOMIC_ACQUIRE) != 0u)
-        ++sv->first_open;
+    advance_first_open(sv);
     if (sv->first_open >= sv->count || __atomic_load_n(sv->h_stop, __ATOMIC_RELAXED)) return FLR_OK;
     flr::FusedArgs a = sv->plan->base;
     a.sources = sv->d_src;
@@ -1065,8 +1070,9 @@ int flr_server_pump(flr_server *sv, void *stream) {
     return FLR_OK;
 }
 
-int flr_server_info(const flr_server *sv, long long *info, int n_info) {
+int flr_server_info(flr_server *sv, long long *info, int n_info) {
     if (!sv || !info) return fail(FLR_E_INVALID_ARGUMENT, "NULL argument");
+    advance_first_open(sv);
     const long long vals[] = {sv->count, sv->items, sv->first_open, sv->launches,
                               sv->launched ? 1LL : 0LL};
     for (int i = 0; i < n_info && i < 5; ++i) info[i] = vals[i];

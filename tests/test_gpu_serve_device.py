@@ -84,13 +84,13 @@ def test_device_loop_rejects_bad_requests(gpu_lib):
     with flr.DeviceLoopServer(0.1, orbits=flr.EqualArmlengthOrbits(t_max=1e6), capacity=2,
                               idle_seconds=0.01) as srv:
         prm = (1e-22, 2e-3, 1e-14, 0.3, 0.1, 0.2, 1.0, 0.5)
-        with pytest.raises(flr.FLRError):
+        with pytest.raises(ValueError, match="tdi_start < n/2"):
             srv.submit(prm, 1000, tdi_set=0)  # shorter than both edge zones
-        with pytest.raises(flr.FLRError):
+        with pytest.raises(ValueError, match="tdi_set"):
             srv.submit(prm, 30000, tdi_set=5)  # no such TDI set
         a = srv.submit(prm, 30000)
         b = srv.submit(prm, 30000, tdi_set=1)
-        with pytest.raises(flr.FLRError, match="full"):
+        with pytest.raises(ValueError, match="full"):
             srv.submit(prm, 30000)
         a.result(timeout=30)
         b.result(timeout=30)
