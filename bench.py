@@ -495,6 +495,21 @@ def run_headline(args, device, peaks, rank, world):
                 "achieved_gbs": fused_bytes / launch_secs / 1e9, "peak_gbs": hbm_peak,
                 "frac": (fused_bytes / launch_secs / 1e9 / hbm_peak) if hbm_peak else None},
     }
+    if traffic and traffic.get("warp_instructions_per_output_sample"):
+        # issue slots: the kernel's warp instructions per sample (ncu, the
+        # first 64 sources) x samples / launch time against 4 schedulers x SMs
+        # x the SM clock sampled during the timed steps
+        sms = torch.cuda.get_device_properties(device).multi_processor_count
+        mhz = res["clocks"].get("sm_mhz") or res["clocks"].get("sm_max_mhz")
+        wips = traffic["warp_instructions_per_output_sample"]
+        if mhz:
+            res["roofline"]["issue"] = {
+                "warp_instructions_per_sample": wips,
+                "achieved_g_per_s": wips * n_out / launch_secs / 1e9,
+                "peak_g_per_s": 4 * sms * mhz * 1e6 / 1e9,
+                "frac": wips * n_out / launch_secs / (4 * sms * mhz * 1e6),
+                "ncu_fp64_pipe_active": traffic.get("fp64_pipe_active"),
+                "ncu_issue_active": traffic.get("issue_active")}
 
     # --- e2e: host memory in and out through run_host (grouped launches)
     # (two page-locked regions, one view per source: the inputs and the channels)
