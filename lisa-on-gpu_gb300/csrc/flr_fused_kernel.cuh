@@ -863,11 +863,14 @@ __device__ __forceinline__ void d2_group_sums(float e32, const df::f2 *edf, int 
 // The grouped form: the same weights for the virtual rows of the three
 // channels (offsets off[c] into y / dd, signs sg[c], 0 = no term).  tab: the
 // partial sums of d2_group_sums for this e32 when the caller has them (the
-// same values), else nullptr.
+// same values), else nullptr.  Adds each channel's signed linear part
+// (double-float) to lin[c] and its signed FP32 correction A acc + sigma l to
+// corr[c]: the caller sums the corrections of all groups in FP32 and adds
+// them to the double-float sum of the linear parts once.
 __device__ __forceinline__ void d2_interp_group(const float2 *y, const float *dd, const int off[3],
                                                 const float sg[3], int d, df::f2 e,
                                                 const D2Weights &w, const df::f2 *edf, int h,
-                                                const float2 *tab, df::f2 out[3]) {
+                                                const float2 *tab, df::f2 lin[3], float corr[3]) {
     const df::f2 ome = df::one_minus(e);
     float acc[3] = {0.f, 0.f, 0.f};
     const float *up[3], *dn[3];
@@ -902,8 +905,10 @@ __device__ __forceinline__ void d2_interp_group(const float2 *y, const float *dd
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const df::f2 v = d2_combine(d2_linear(y + off[k], d, e, ome), w, acc[k]);
-        out[k] = (sg[k] == 0.f) ? df::f2{0.f, 0.f} : df::f2{sg[k] * v.hi, sg[k] * v.lo};
+        if (sg[k] == 0.f) continue;
+        const df::f2 l = d2_linear(y + off[k], d, e, ome);
+        lin[k] = df::add(lin[k], {sg[k] * l.hi, sg[k] * l.lo});
+        corr[k] = __fmaf_rn(sg[k], __fmaf_rn(w.A, acc[k], w.sigma * l.hi), corr[k]);
     }
 }
 
@@ -1814,9 +1819,10 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
         // second differences in the input window's space.
         const size_t tab_off = lay.d2 + align128(sizeof(float) * 6 * (size_t)a.y_max);
         float *wkey = reinterpret_cast<float *>(smem + tab_off);
-        float2 *wtab = reinterpret_cast<float2 *>(smem + tab_off + 256);
+        float2 *was = reinterpret_cast<float2 *>(smem + tab_off + 256);  // (A, sigma) per key
+        float2 *wtab = reinterpret_cast<float2 *>(smem + tab_off + 256 + 512);
         const bool use_tab = kGrouped && kD2 && o0 < o1 &&
-                             tab_off + 256 + sizeof(float2) * 3 * kFusedMaxGroups * (h - 1) <=
+                             tab_off + 768 + sizeof(float2) * 3 * kFusedMaxGroups * (h - 1) <=
                                  lay.y;
         if (kMixed && kD2) {
             second_differences(y32, d2, kGrouped ? set->num_vrows : 6, Y, a.y_max, tid, kThreads);
@@ -1836,6 +1842,8 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
                 // NaN key, which no sample matches)
                 const float key = __int_as_float(__float_as_int(e.hi) + (v - 1));
                 wkey[tid] = key;
+                const D2Weights wk = d2_weights(a, inv_deps_df, df::f2{key, 0.f});
+                was[tid] = make_float2(wk.A, wk.sigma);
                 d2_group_sums(key, edf, h, wtab + (size_t)tid * (h - 1));
             }
             __syncthreads();
@@ -1852,6 +1860,7 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
                     (w.w < 0) ? 0.0
                               : orbit_lerp_b(a.orb.ltt, a.orb.ltt_slope, w.w, 6, 0, t, w.base);
                 df::f2 accdf[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+                float corr[3] = {0.f, 0.f, 0.f};  // the difference form's FP32 parts
                 double delay = t;
                 int depth = 0;
                 for (int g = 0; g < set->num_groups; ++g) {
@@ -1879,27 +1888,39 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
                         off[c] = set->group_vrow[g][c] * a.y_max;
                         sg[c] = set->group_vsign[g][c];
                     }
-                    df::f2 val[3];
                     if (kD2) {
-                        const D2Weights w2 = d2_weights(a, inv_deps_df, e_df);
-                        const float2 *tab = nullptr;
-                        if (use_tab) {
-                            const float k32 = e_df.hi;
-                            const int q = (k32 == wkey[3 * g + 1])   ? 3 * g + 1
-                                          : (k32 == wkey[3 * g])     ? 3 * g
-                                          : (k32 == wkey[3 * g + 2]) ? 3 * g + 2
-                                                                     : -1;
-                            if (q >= 0) tab = wtab + (size_t)q * (h - 1);
+                        // the FP32 weights, A and sigma are functions of eps
+                        // rounded to FP32 (tabulated per item, or computed)
+                        const float k32 = e_df.hi;
+                        int q = -1;
+                        if (use_tab)
+                            q = (k32 == wkey[3 * g + 1])   ? 3 * g + 1
+                                : (k32 == wkey[3 * g])     ? 3 * g
+                                : (k32 == wkey[3 * g + 2]) ? 3 * g + 2
+                                                           : -1;
+                        D2Weights w2;
+                        if (q >= 0) {
+                            const float2 as = was[q];
+                            w2.A = as.x;
+                            w2.sigma = as.y;
+                        } else {
+                            w2 = d2_weights(a, inv_deps_df, df::f2{k32, 0.f});
                         }
-                        d2_interp_group(y32, d2, off, sg, (int)(d - ya), e_df, w2, edf, h, tab,
-                                        val);
+                        d2_interp_group(y32, d2, off, sg, (int)(d - ya), e_df, w2, edf, h,
+                                        q >= 0 ? wtab + (size_t)q * (h - 1) : nullptr, accdf,
+                                        corr);
                     } else {
+                        df::f2 val[3];
                         const df::f2 A_df = prefactor_df(a.a_tab, a.lt.num_A, inv_deps_df, e_df);
                         df_interp_group(y32, off, sg, (int)(d - ya), A_df, e_df, edf, h, a.h_df,
                                         val);
-                    }
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) accdf[c] = df::add(accdf[c], val[c]);
+                        for (int c = 0; c < 3; ++c) accdf[c] = df::add(accdf[c], val[c]);
+                    }
+                }
+                if (kD2) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) accdf[c] = df::add(accdf[c], {corr[c], 0.f});
                 }
                 const double X = df::to_double_bits(accdf[0], -sexp);
                 const double Yc = df::to_double_bits(accdf[1], -sexp);
