@@ -477,12 +477,33 @@ struct DfProjection {
 // Projection factors of one link (LISAResponse.cu:581-606, 664) in df from the
 // FP64 spacecraft positions: n = (x_rec - x_em) / |x_rec - x_em|,
 // xi+ = ((u.n)^2 - (v.n)^2) / 2, xix = (u.n)(v.n), 1 / (1 - k.n).
+__device__ __forceinline__ DfProjection df_projection_of(df::f2 n[3], const df::f2 k[3],
+                                                         const df::f2 u[3], const df::f2 v[3]);
+
 __device__ __forceinline__ DfProjection df_projection(const double x_rec[3], const double x_em[3],
                                                       const df::f2 k[3], const df::f2 u[3],
                                                       const df::f2 v[3]) {
     df::f2 n[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) n[c] = df::from_double_bits(x_rec[c] - x_em[c]);
+    return df_projection_of(n, k, u, v);
+}
+
+// The same from double-float positions: the link vector as a double-float
+// difference (~1e-13 of it, where the projection factors need ~1e-11), which
+// takes three FP64 subtractions per link off the FP64 pipe.
+__device__ __forceinline__ DfProjection df_projection_df(const df::f2 x_rec[3],
+                                                         const df::f2 x_em[3], const df::f2 k[3],
+                                                         const df::f2 u[3], const df::f2 v[3]) {
+    df::f2 n[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) n[c] = df::sub(x_rec[c], x_em[c]);
+    return df_projection_of(n, k, u, v);
+}
+
+// n: the link vector x_rec - x_em (overwritten)
+__device__ __forceinline__ DfProjection df_projection_of(df::f2 n[3], const df::f2 k[3],
+                                                         const df::f2 u[3], const df::f2 v[3]) {
     const df::f2 r = df_rsqrt(df_dot3(n, n));
 #pragma unroll
     for (int c = 0; c < 3; ++c) n[c] = df::mul(n[c], r);
@@ -1413,14 +1434,24 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
         double scale = 1.0;
         int sexp = 0;
         if (kMixed) {
-            double m = 0.0;
+            // the window's largest magnitude, from the bits (non-negative
+            // doubles order like their bit patterns; NaN is skipped as fmax
+            // skips it): integer work instead of FP64 comparisons
+            unsigned long long mb = 0ull;
             for (int i = tid; i < W; i += kThreads) {
-                double2 q = hraw[i];
-                m = fmax(m, fmax(fabs(q.x), fabs(q.y)));
+                const double2 q = hraw[i];
+                unsigned long long bx = (unsigned long long)__double_as_longlong(q.x) &
+                                        0x7fffffffffffffffull;
+                unsigned long long by = (unsigned long long)__double_as_longlong(q.y) &
+                                        0x7fffffffffffffffull;
+                if (bx > 0x7ff0000000000000ull) bx = 0ull;
+                if (by > 0x7ff0000000000000ull) by = 0ull;
+                mb = max(mb, max(bx, by));
             }
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
-            if ((tid & 31) == 0) warp_max[tid >> 5] = m;
+            for (int off = 16; off > 0; off >>= 1)
+                mb = max(mb, (unsigned long long)__shfl_xor_sync(0xffffffffu, mb, off));
+            if ((tid & 31) == 0) warp_max[tid >> 5] = __longlong_as_double((long long)mb);
             __syncthreads();
             if (tid == 0) {
                 double mm = 0.0;
@@ -1479,6 +1510,7 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
                 ReceiverSide rs{};
                 EmitterSide es{};
                 df::f2 re_r = {0.f, 0.f}, im_r = {0.f, 0.f}, re_e = {0.f, 0.f}, im_e = {0.f, 0.f};
+                df::f2 xr_df[3] = {}, xe_df[3] = {};  // positions for the projections
                 bool ok_r = false, ok_e = false;
                 if (live) {
                     rs = receiver_mixed(a.orb, a.inv_orbit_dt, rr + 1, t, t0, a.fs, k, segc);
@@ -1488,6 +1520,11 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
                                        segc);
                     ok_e = mixed_interp_any<kD2>(a, hdf, dh, wlo, W, hsrc, scale, n, es.d_em,
                                             es.e_em, inv_deps_df, edf, h, re_e, im_e);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        xr_df[c] = df::from_double_bits(rs.x_rec[c]);
+                        xe_df[c] = df::from_double_bits(es.x_em[c]);
+                    }
                 }
                 const bool own = live && (j >= o0 && j < o1);  // diagnostics
                 for (int q = 0; q < 2; ++q) {
@@ -1499,9 +1536,11 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
                     const df::f2 xim = {__shfl_sync(full, im_e.hi, from),
                                         __shfl_sync(full, im_e.lo, from)};
                     const bool xok = __shfl_sync(full, (int)ok_e, from) != 0;
-                    double x_em[3];
+                    df::f2 x_em[3];
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) x_em[c] = __shfl_sync(full, es.x_em[c], from);
+                    for (int c = 0; c < 3; ++c)
+                        x_em[c] = {__shfl_sync(full, xe_df[c].hi, from),
+                                   __shfl_sync(full, xe_df[c].lo, from)};
                     const int d_em = __shfl_sync(full, es.d_em, from);
                     if (!act) continue;
                     if (!live) {  // the reference's y_gw is zero there
@@ -1517,7 +1556,7 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
                         y32[slot * a.y_max + jj] = make_float2(__int_as_float(0x7fc00000), 0.f);
                         continue;
                     }
-                    const DfProjection pr = df_projection(rs.x_rec, x_em, kdf, udf, vdf);
+                    const DfProjection pr = df_projection_df(xr_df, x_em, kdf, udf, vdf);
                     const df::f2 dre = df::sub(xre, re_r), dim = df::sub(xim, im_r);
                     df::f2 yv = df::add(df::mul(dre, pr.xi_p), df::mul(dim, pr.xi_c));
                     yv = df::mul(yv, pr.pre);
