@@ -130,15 +130,27 @@ class DeviceLoopServer:
         self._done = np.frombuffer((ctypes.c_uint32 * self.capacity).from_address(flags),
                                    dtype=np.uint32)
         self.stream = torch.cuda.Stream(device=self.device)
-        self._pending = {}  # slot -> output tensor, kept alive until its tiles are written
+        self._pending = {}  # slot -> (output, stored waveform), kept alive until written
 
     # -- requests --------------------------------------------------------------
     def submit(self, params, n: int, tdi_set: int = 0, t0: float = 0.0, model: str = "config",
-               out=None) -> DeviceTicket:
+               out=None, h=None) -> DeviceTicket:
         """Submit one request: ``params`` = (A, f, fdot, iota, phi0, psi, lam,
-        beta), ``n`` samples from ``t0``.  ``out`` (optional) receives the
-        (3, n) float64 channels on this server's device."""
+        beta), ``n`` samples from ``t0``; the waveform is generated inside the
+        kernel from the first six.  With ``h`` (a contiguous complex128 CUDA
+        tensor of n samples on this device, kept alive until the request is
+        done) the stored waveform is used instead and only lam, beta are read
+        from ``params``.  ``out`` (optional) receives the (3, n) float64
+        channels on this server's device.  The running kernel reads ``h`` and
+        writes ``out`` as soon as the request is published, outside any
+        stream order, so when either is given ``submit`` first waits for the
+        work queued on the current stream (which may still write ``h`` or
+        read ``out``)."""
         n = int(n)
+        if h is not None and (tuple(h.shape) != (n,) or h.dtype != torch.complex128
+                              or not h.is_cuda or not h.is_contiguous()):
+            raise ValueError(f"h must be a contiguous ({n},) complex128 CUDA tensor")
+        caller_out = out is not None
         if out is None:
             with torch.cuda.device(self.device), torch.cuda.stream(self.stream):
                 out = torch.empty((3, n), dtype=torch.float64, device=self.device)
@@ -146,6 +158,7 @@ class DeviceLoopServer:
               or not out.is_contiguous()):
             raise ValueError(f"out must be a contiguous (3, {n}) float64 CUDA tensor")
         src = np.zeros(1, dtype=SOURCE_DTYPE)
+        src["h"] = 0 if h is None else h.data_ptr()
         src["out"] = out.data_ptr()
         src["n"] = n
         src["projections_start"] = self.plan.projections_start_ind
@@ -153,15 +166,22 @@ class DeviceLoopServer:
         src["t0"] = float(t0)
         src["k"][0], src["u"][0], src["v"][0] = sky_basis(float(params[6]), float(params[7]))
         src["tdi_set"] = int(tdi_set)
-        gb = np.zeros(1, dtype=GB_DTYPE)
-        for j, key in enumerate(("A", "f", "fdot", "iota", "phi0", "psi")):
-            gb[key] = float(params[j])
-        gb["model"] = GB_MODELS[model]
+        if h is not None or caller_out:
+            ev = torch.cuda.Event()
+            ev.record(torch.cuda.current_stream(self.device))
+            ev.synchronize()
+        gb_ptr = None
+        if h is None:
+            gb = np.zeros(1, dtype=GB_DTYPE)
+            for j, key in enumerate(("A", "f", "fdot", "iota", "phi0", "psi")):
+                gb[key] = float(params[j])
+            gb["model"] = GB_MODELS[model]
+            gb_ptr = gb.ctypes.data
         slot = ctypes.c_int()
         with torch.cuda.device(self.device):
-            _lib.check(self._lib.flr_server_submit(self._srv, src.ctypes.data, gb.ctypes.data,
+            _lib.check(self._lib.flr_server_submit(self._srv, src.ctypes.data, gb_ptr,
                                                    ctypes.byref(slot)))
-        self._pending[slot.value] = out
+        self._pending[slot.value] = (out, h)
         self.pump()
         return DeviceTicket(self, slot.value, out)
 

@@ -78,6 +78,34 @@ def test_device_loop_matches_batch(gpu_lib, orbit_kind, chan):
         assert srv.status() == 0
 
 
+def test_device_loop_stored_waveforms(gpu_lib):
+    """Requests with a stored waveform (h) beside generated ones: the bits of
+    a batch run of the same waveforms."""
+    import torch
+
+    import fastlisaresponse_gb300 as flr
+
+    dt = 10.0
+    orb = flr.KeplerianOrbits(t_max=2e6)
+    rng = np.random.default_rng(83)
+    reqs = _requests(rng, 6, 2**13, 2**16, 2)
+    with flr.DeviceLoopServer(1 / dt, orbits=orb, capacity=16, idle_seconds=0.05) as srv:
+        hs, tickets = [], []
+        for r in reqs:
+            t = r["t0"] + torch.arange(r["n"], dtype=torch.float64, device=srv.device) * dt
+            hs.append(flr.gb_waveform(*r["params"][:6], t))
+            tickets.append(srv.submit(r["params"], r["n"], r["tdi_set"], r["t0"], h=hs[-1]))
+        got = [t.result(timeout=60) for t in tickets]
+        want = srv.plan(hs, [r["params"][6] for r in reqs], [r["params"][7] for r in reqs],
+                        t0=[r["t0"] for r in reqs], tdi_set=[r["tdi_set"] for r in reqs])
+        torch.cuda.synchronize()
+        for g, w in zip(got, want):
+            assert torch.equal(g, w)
+        with pytest.raises(ValueError, match="complex128"):
+            srv.submit(reqs[0]["params"], reqs[0]["n"] + 1, h=hs[0])
+        assert srv.status() == 0
+
+
 def test_device_loop_rejects_bad_requests(gpu_lib):
     import fastlisaresponse_gb300 as flr
 
