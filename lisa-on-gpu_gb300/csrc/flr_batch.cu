@@ -538,7 +538,7 @@ int flr_batch_plan_create(flr_orbits *orbits, int order, const double *A_in, dou
             s.delay_len[u] = len;
             int keep = 0;
             if (u > 0) {
-                const int lim = std::min(len, s.delay_len[u - 1]);
+                const int lim = std::min(len, (int)s.delay_len[u - 1]);
                 if (mixed && equal_arms)
                     keep = lim;  // every L(t) is the same value: partial sums depend on length only
                 else

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdint>
+
 #include "flr_device.cuh"
 
 namespace flr {
@@ -52,24 +54,28 @@ struct FusedSource {
 };
 
 // TDI unit tables with link numbers already mapped to link slots.
+// Small integer fields in the narrowest types that hold their ranges (link
+// slots 0-5, channels 0-2, list lengths <= kFusedMaxDepth, unit and entry
+// counts <= kFusedMaxUnits / kFusedMaxCombos; the plan checks them): each
+// block keeps the set in shared memory, where its size limits the tile.
 struct FusedTdiSet {
     int num_units;
     int num_combos;
-    int unit_start[kFusedMaxUnits];
-    int unit_len[kFusedMaxUnits];
-    int base_slot[kFusedMaxUnits];
-    int channel[kFusedMaxUnits];
     double sign[kFusedMaxUnits];
-    int sign_code[kFusedMaxUnits];    // +1, -1, or 0 (general sign: multiply)
+    int16_t unit_start[kFusedMaxUnits];
+    int16_t unit_len[kFusedMaxUnits];
+    int8_t base_slot[kFusedMaxUnits];
+    int8_t channel[kFusedMaxUnits];
+    int8_t sign_code[kFusedMaxUnits];    // +1, -1, or 0 (general sign: multiply)
     // Delay lists in compact form: unit u subtracts L of link_slot[u][0..len-1]
     // (the "no delay" markers removed), and shares its first prefix_keep[u]
     // partial sums with unit u-1, whose partial sums are bitwise the ones u
     // would compute itself (same subtractions in the same order).
-    int delay_len[kFusedMaxUnits];
-    int prefix_keep[kFusedMaxUnits];
-    int orig_unit[kFusedMaxUnits];    // position of the unit in the caller's table
-    int delay_slot[kFusedMaxUnits][kFusedMaxDepth];
-    int combo_slot[kFusedMaxCombos];  // -1: no delay
+    int8_t delay_len[kFusedMaxUnits];
+    int8_t prefix_keep[kFusedMaxUnits];
+    int8_t orig_unit[kFusedMaxUnits];    // position of the unit in the caller's table
+    int8_t delay_slot[kFusedMaxUnits][kFusedMaxDepth];
+    int8_t combo_slot[kFusedMaxCombos];  // -1: no delay
     // Grouped form, for mixed arithmetic on equal-arm orbits, where every L(t)
     // is the same value and units with delay lists of equal length have
     // bitwise-equal delays.  Group g holds the units [group_start[g],
@@ -84,13 +90,16 @@ struct FusedTdiSet {
     int grouped;
     int num_groups;
     int num_vrows;
-    int group_len[kFusedMaxGroups];
-    int group_start[kFusedMaxGroups + 1];
-    int group_vrow[kFusedMaxGroups][3];
     float group_vsign[kFusedMaxGroups][3];
-    int vrow_a[6], vrow_b[6];
     float vrow_ca[6], vrow_cb[6];
+    int8_t group_len[kFusedMaxGroups];
+    int8_t group_start[kFusedMaxGroups + 1];
+    int8_t group_vrow[kFusedMaxGroups][3];
+    int8_t vrow_a[6], vrow_b[6];
 };
+static_assert(kFusedMaxUnits <= 127 && kFusedMaxDepth <= 127 && kFusedMaxCombos <= 32767,
+              "FusedTdiSet field types");
+static_assert(sizeof(FusedTdiSet) % sizeof(int) == 0, "the set is copied as ints");
 
 enum FusedChan { kChanXYZ = 0, kChanAET = 1, kChanAE = 2 };
 

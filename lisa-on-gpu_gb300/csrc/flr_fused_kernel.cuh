@@ -123,24 +123,30 @@ __host__ __device__ inline Layout layout(bool mixed, int win_max, int y_max) {
     off = align128(off + sizeof(FusedTdiSet));
     L.edf = off;
     off = align128(off + sizeof(df::f2) * kFusedMaxH);
-    L.hraw = off;
-    off = align128(off + sizeof(double2) * (size_t)win_max);
     if (mixed) {
+        // the raw window is read only until its double-float copy and
+        // differences exist, before the link stage writes its rows: it shares
+        // their space; the TDI stage's second differences (6 * y_max floats
+        // <= win_max * 32 bytes, since win_max >= y_max) and weight tables
+        // then take the space of the window's copies
         L.hdf = off;
         off = align128(off + sizeof(float4) * (size_t)win_max);
         L.dh = off;
         off = align128(off + sizeof(float4) * (size_t)win_max);
         L.y = off;
-        off = align128(off + sizeof(float2) * 6 * (size_t)y_max);
+        L.hraw = off;
+        const size_t rows = sizeof(float2) * 6 * (size_t)y_max;
+        const size_t raw = sizeof(double2) * (size_t)win_max;
+        off = align128(off + (rows > raw ? rows : raw));
+        L.d2 = L.hdf;
     } else {
+        L.hraw = off;
+        off = align128(off + sizeof(double2) * (size_t)win_max);
         L.hdf = L.dh = 0;
         L.y = off;
         off = align128(off + sizeof(double) * 6 * (size_t)y_max);
+        L.d2 = L.hraw;
     }
-    // mixed: the six rows of second differences of the TDI stage take the
-    // input window's space, which the link stage no longer needs by then
-    // (6 * y_max floats <= win_max * 48 bytes, since win_max >= y_max)
-    L.d2 = L.hraw;
     L.total = off;
     return L;
 }

@@ -31,7 +31,7 @@ from typing import Dict, Optional, Sequence
 
 import numpy as np
 
-TILE_CANDIDATES = (128, 256, 512, 1024, 2048)
+TILE_CANDIDATES = (128, 256, 512, 768, 1024, 2048)
 DEFAULT_TUNE_LENGTHS = (2**18,) * 32
 
 _memo: Dict[str, dict] = {}
