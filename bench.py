@@ -985,13 +985,15 @@ def run_profile_batch(spec: str) -> None:
     equal-arm or Keplerian orbits; kind batch64: the first 64 sources of the
     batching configuration (49.3 M samples, 2.0 GB of inputs and outputs).
     2nd-gen TDI XYZ, order 25; plain:<equal|kepler>: the plain FP64 drop-in
-    path (pyResponseTDI) on one source of 2^21 samples at dt = 5 s.  Two
-    calls (the capture takes the first)."""
+    path (pyResponseTDI) on one source of 2^21 samples at dt = 5 s.  An
+    optional third field sets the tile of the batched cases (default: the
+    library's).  Two calls (the capture takes the first)."""
     import torch
 
     import fastlisaresponse_gb300 as flr
 
-    prec, kind = spec.split(":")
+    prec, kind, *rest = spec.split(":")
+    tile = int(rest[0]) if rest else 0
     dev = torch.device("cuda", 0)
     if prec == "plain":
         # the plain FP64 drop-in path on one source of 2^21 samples at dt = 5 s
@@ -1029,7 +1031,7 @@ def run_profile_batch(spec: str) -> None:
                               p["psi"][i], t) for i in range(ns)]
         lam, beta = p["lam"], p["beta"]
     bat = flr.BatchedResponseTDI(1 / dt, order=25, tdi="2nd generation", orbits=orb,
-                                 precision=prec)
+                                 precision=prec, tile=tile)
     for _ in range(2):
         bat(hs, lam, beta)
     torch.cuda.synchronize()
