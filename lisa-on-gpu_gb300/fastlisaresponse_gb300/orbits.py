@@ -251,17 +251,16 @@ def read_lisa_orbits(path, armlength=2.5e9, h5py_module=None) -> Orbits:
     the order 12, 23, 31, 13, 32, 21, and the root attributes ``dt`` [s] and
     ``size`` (N); knot i is at i * dt.
 
-    h5py is not a dependency of this package: it is imported here, or pass a
-    module with h5py's ``File`` interface as ``h5py_module``.  The tables can
-    also be read by any other HDF5 reader and given to ``Orbits(t, x, ltt,
-    n)`` directly."""
+    The file is read with h5py when it is installed, else with this
+    package's own reader (:mod:`.h5lite`, the HDF5 structures h5py writes by
+    default); ``h5py_module`` overrides both with any module that has h5py's
+    ``File`` interface.  The tables can also be read by any other HDF5 reader
+    and given to ``Orbits(t, x, ltt, n)`` directly."""
     if h5py_module is None:
         try:
             import h5py as h5py_module
-        except ImportError as e:
-            raise ImportError("reading LISA Orbits files needs h5py; or read the datasets "
-                              "tcb/x, tcb/ltt, tcb/n with another HDF5 reader and pass them to "
-                              "Orbits(t, x, ltt, n)") from e
+        except ImportError:
+            from . import h5lite as h5py_module
     with h5py_module.File(path, "r") as f:
         dt = float(f.attrs["dt"])
         size = int(f.attrs["size"])
