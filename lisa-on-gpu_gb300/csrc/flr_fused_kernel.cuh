@@ -307,6 +307,15 @@ __device__ __forceinline__ void split_delay_df(double delayed_t, double t_first,
     eps = df::from_double((double)c - x);
 }
 
+// k . x for a delay: ((a0 b0) + a1 b1) + a2 b2.  The reference's
+// dot_product_1d (LISAResponse.cu:48-57) starts from 0 + a0 b0, which differs
+// from a0 b0 only when a0 b0 is -0; the two sums then differ at most in the
+// sign of a zero result, and t - (+-0) C^-1 is the same delayed time, so the
+// index split gets the same bits with one FP64 addition fewer.
+__device__ __forceinline__ double dot3_delay(const double *a, const double *b) {
+    return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
+}
+
 struct MixedDelays {
     int d_rec, d_em;
     df::f2 e_rec, e_em;
@@ -325,8 +334,8 @@ __device__ __forceinline__ MixedDelays link_delays_mixed(const OrbitTables &o, d
     double t_em = t - L;
     position_seg(o, w, t, o.sc_r[slot], g.x_rec);
     position_seg(o, orbit_segment_fast(o, inv_dt, t_em), t_em, o.sc_e[slot], g.x_em);
-    double kx_rec = dot3(k, g.x_rec);
-    double kx_em = dot3(k, g.x_em);
+    double kx_rec = dot3_delay(k, g.x_rec);
+    double kx_em = dot3_delay(k, g.x_em);
     split_delay_df(t - kx_rec * kCInv, t_first, fs, g.d_rec, g.e_rec);
     split_delay_df(t_em - kx_em * kCInv, t_first, fs, g.d_em, g.e_em);
     return g;
@@ -348,7 +357,7 @@ __device__ __forceinline__ ReceiverSide receiver_mixed(const OrbitTables &o, dou
     ReceiverSide r;
     r.w = seg_of(sc_, o, inv_dt, t);
     position_sb(o, r.w, t, sc, r.x_rec);
-    split_delay_df(t - dot3(k, r.x_rec) * kCInv, t_first, fs, r.d_rec, r.e_rec);
+    split_delay_df(t - dot3_delay(k, r.x_rec) * kCInv, t_first, fs, r.d_rec, r.e_rec);
     return r;
 }
 
@@ -368,7 +377,7 @@ __device__ __forceinline__ EmitterSide emitter_mixed(const OrbitTables &o, doubl
         (w.w < 0) ? 0.0 : orbit_lerp_b(o.ltt, o.ltt_slope, w.w, 6, slot, t, w.base);
     const double t_em = t - L;
     position_sb(o, seg_of(sc_, o, inv_dt, t_em), t_em, o.sc_e[slot], e.x_em);
-    split_delay_df(t_em - dot3(k, e.x_em) * kCInv, t_first, fs, e.d_em, e.e_em);
+    split_delay_df(t_em - dot3_delay(k, e.x_em) * kCInv, t_first, fs, e.d_em, e.e_em);
     return e;
 }
 
