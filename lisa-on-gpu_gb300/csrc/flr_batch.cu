@@ -87,6 +87,7 @@ struct flr_batch_graph {
     unsigned char *h_stage[2];  // pinned staging, alternated between launches
     unsigned char *d_stage;
     cudaGraphExec_t exec[2];    // exec[b] copies from h_stage[b]
+    cudaGraphExec_t exec_t0[2]; // the same with the t0 = 0 instance (or null)
     cudaEvent_t done[2];        // recorded after the launch that used buffer b
     bool pending[2];
     int next;                   // buffer of the next launch
@@ -383,10 +384,23 @@ int fill_stage(const flr_batch_plan *plan, const flr_batch_source *sources, int 
     return FLR_OK;
 }
 
-// The copy of a staging image to `d_stage` and the kernels that read it.
+// Whether every source starts at t0 = +0 (its bit pattern is 0): such
+// launches may take the fused kernel's t0 = 0 instance.
+bool all_t0_zero(const flr_batch_source *sources, int num_sources) {
+    for (int i = 0; i < num_sources; ++i) {
+        unsigned long long bits;
+        std::memcpy(&bits, &sources[i].t0, sizeof(bits));
+        if (bits != 0ull) return false;
+    }
+    return num_sources > 0;
+}
+
+// The copy of a staging image to `d_stage` and the kernels that read it
+// (t0_zero: every staged source starts at t0 = +0).
 cudaError_t enqueue(const flr_batch_plan *plan, const unsigned char *h_stage,
                     unsigned char *d_stage, const StageLayout &lay, int cap, bool waveforms,
-                    bool diag, double *partial, int chan, cudaEvent_t copied, cudaStream_t st) {
+                    bool diag, double *partial, int chan, bool t0_zero, cudaEvent_t copied,
+                    cudaStream_t st) {
     cudaError_t err = cudaMemcpyAsync(d_stage, h_stage, lay.bytes, cudaMemcpyHostToDevice, st);
     if (err == cudaSuccess && copied) err = cudaEventRecord(copied, st);
     if (err != cudaSuccess) return err;
@@ -411,7 +425,7 @@ cudaError_t enqueue(const flr_batch_plan *plan, const unsigned char *h_stage,
     // whose absolute error stays ~1e-14 of the links: those channels are
     // combinations of X, Y, Z that can cancel to a small fraction of them
     const bool d2 = plan->mixed && plan->base.d2 && chan == FLR_CHAN_XYZ;
-    err = flr::launch_fused(plan->mixed, plan->grouped, diag, partial != nullptr, d2, a,
+    err = flr::launch_fused(plan->mixed, plan->grouped, diag, partial != nullptr, d2, t0_zero, a,
                             plan->grid_max,
                             plan->smem, st);
     if (err == cudaSuccess && partial) err = flr::launch_inner_reduce(a, st);
@@ -422,6 +436,7 @@ void release_graph(flr_batch_graph *g) {
     if (!g) return;
     for (int b = 0; b < 2; ++b) {
         if (g->exec[b]) cudaGraphExecDestroy(g->exec[b]);
+        if (g->exec_t0[b]) cudaGraphExecDestroy(g->exec_t0[b]);
         if (g->h_stage[b]) cudaFreeHost(g->h_stage[b]);
         if (g->done[b]) cudaEventDestroy(g->done[b]);
     }
@@ -804,7 +819,8 @@ static int batch_run(flr_batch_plan *plan, const flr_batch_source *sources, int 
         plan->cap_partial = partial_bytes + partial_bytes / 2;
     }
     err = enqueue(plan, plan->h_stage, plan->d_stage, lay, num_sources, gb != nullptr, diag,
-                  inner ? plan->d_partial : nullptr, chan, plan->stage_free, st);
+                  inner ? plan->d_partial : nullptr, chan, all_t0_zero(sources, num_sources),
+                  plan->stage_free, st);
     plan->stage_pending = true;
     if (err != cudaSuccess) return cuda_fail(err, "launching the batch");
     err = cudaEventRecord(plan->done, st);
@@ -855,15 +871,21 @@ int flr_batch_graph_create(flr_batch_plan *plan, int max_sources, int flags, int
     }
     cudaStream_t cs = nullptr;
     if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
-    for (int b = 0; b < 2 && err == cudaSuccess; ++b) {
+    // per staging buffer, the general launch and (where the difference-form
+    // instance runs) the one for sources that all start at t0 = +0
+    const bool with_t0 = plan->mixed && plan->base.d2 && chan == FLR_CHAN_XYZ && !g->diag;
+    for (int v = 0; v < (with_t0 ? 4 : 2) && err == cudaSuccess; ++v) {
+        const int b = v & 1;
         err = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
         if (err != cudaSuccess) break;
         const cudaError_t e_enq = enqueue(plan, g->h_stage[b], g->d_stage, lay, g->cap,
-                                          g->waveforms, g->diag, nullptr, chan, nullptr, cs);
+                                          g->waveforms, g->diag, nullptr, chan, v >= 2, nullptr,
+                                          cs);
         cudaGraph_t graph = nullptr;
         const cudaError_t e_end = cudaStreamEndCapture(cs, &graph);
         err = (e_enq != cudaSuccess) ? e_enq : e_end;
-        if (err == cudaSuccess) err = cudaGraphInstantiate(&g->exec[b], graph, 0);
+        if (err == cudaSuccess)
+            err = cudaGraphInstantiate(v >= 2 ? &g->exec_t0[b] : &g->exec[b], graph, 0);
         if (graph) cudaGraphDestroy(graph);
     }
     if (cs) cudaStreamDestroy(cs);
@@ -911,7 +933,8 @@ int flr_batch_graph_launch(flr_batch_graph *g, const flr_batch_source *sources,
         err = cudaStreamWaitEvent(st, g->done[g->last], 0);
         if (err != cudaSuccess) return cuda_fail(err, "ordering after the previous launch");
     }
-    err = cudaGraphLaunch(g->exec[b], st);
+    const bool t0_zero = g->exec_t0[b] && all_t0_zero(sources, num_sources);
+    err = cudaGraphLaunch(t0_zero ? g->exec_t0[b] : g->exec[b], st);
     if (err == cudaSuccess) err = cudaEventRecord(g->done[b], st);
     if (err != cudaSuccess) return cuda_fail(err, "launching the batch graph");
     g->pending[b] = true;

@@ -10,7 +10,9 @@ size_t fused_smem_bytes(bool mixed, int win_max, int y_max) {
     return layout(mixed, win_max, y_max).total;
 }
 
-static const void *fused_fn(bool mixed, bool grouped, bool diag, bool inner, bool d2) {
+static const void *fused_fn(bool mixed, bool grouped, bool diag, bool inner, bool d2,
+                            bool t0_zero = false) {
+    if (mixed && d2 && t0_zero && !diag && !inner) return fused_fn_t0(grouped);
     if (mixed && d2) return fused_fn_d2(grouped, diag, inner);
     if (inner) {
         if (mixed && grouped)
@@ -30,10 +32,11 @@ static const void *fused_fn(bool mixed, bool grouped, bool diag, bool inner, boo
 }
 
 cudaError_t fused_configure(bool mixed, bool grouped, size_t smem_bytes, int *blocks_per_sm) {
-    // plain, diagnostics, inner products; both forms of the mixed flavour
-    for (int v = 0; v < (mixed ? 6 : 3); ++v) {
-        cudaError_t err = cudaFuncSetAttribute(fused_fn(mixed, grouped, v % 3 == 1, v % 3 == 2,
-                                                        v >= 3),
+    // plain, diagnostics, inner products; both forms of the mixed flavour, and
+    // the difference form's t0 = 0 instance
+    for (int v = 0; v < (mixed ? 7 : 3); ++v) {
+        cudaError_t err = cudaFuncSetAttribute(fused_fn(mixed, grouped, v % 3 == 1 && v < 6,
+                                                        v % 3 == 2, v >= 3, v == 6),
                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)smem_bytes);
         if (err != cudaSuccess) return err;
@@ -42,22 +45,22 @@ cudaError_t fused_configure(bool mixed, bool grouped, size_t smem_bytes, int *bl
     int per = 0;
     cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &per, fused_fn(mixed, grouped, false, false, false), kThreads, smem_bytes);
-    if (err == cudaSuccess && mixed) {
+    for (int v = 0; v < 2 && err == cudaSuccess && mixed; ++v) {
         int per2 = 0;
         err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per2, fused_fn(mixed, grouped, false, false, true), kThreads, smem_bytes);
+            &per2, fused_fn(mixed, grouped, false, false, true, v == 1), kThreads, smem_bytes);
         per = std::min(per, per2);
     }
     *blocks_per_sm = per;
     return err;
 }
 
-cudaError_t launch_fused(bool mixed, bool grouped, bool diag, bool inner, bool d2,
+cudaError_t launch_fused(bool mixed, bool grouped, bool diag, bool inner, bool d2, bool t0_zero,
                          const FusedArgs &a, int grid, size_t smem_bytes, cudaStream_t stream) {
     if (a.num_sources <= 0) return cudaSuccess;
     if (diag && inner) return cudaErrorInvalidValue;
     void *args[] = {const_cast<FusedArgs *>(&a)};
-    return cudaLaunchKernel(fused_fn(mixed, grouped, diag, inner, d2), dim3(grid),
+    return cudaLaunchKernel(fused_fn(mixed, grouped, diag, inner, d2, t0_zero), dim3(grid),
                             dim3(kThreads), args, smem_bytes, stream);
 }
 

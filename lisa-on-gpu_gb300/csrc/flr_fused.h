@@ -199,11 +199,17 @@ cudaError_t fused_configure(bool mixed, bool grouped, size_t smem_bytes, int *bl
 cudaError_t launch_inner_reduce(const FusedArgs &a, cudaStream_t stream);
 // diag: the instance that writes the FusedSource diagnostics (more registers);
 // inner: the instance that forms inner products (FusedArgs::partial set);
-// d2: the mixed instance in difference form (FusedArgs::d2 tables required).
-cudaError_t launch_fused(bool mixed, bool grouped, bool diag, bool inner, bool d2,
+// d2: the mixed instance in difference form (FusedArgs::d2 tables required);
+// t0_zero: every source of the launch has t0 = +0 (bit pattern 0), which
+// selects the difference-form instance without the t0 operations (no
+// diagnostics, no inner products; the other launches ignore it).
+cudaError_t launch_fused(bool mixed, bool grouped, bool diag, bool inner, bool d2, bool t0_zero,
                          const FusedArgs &a, int grid, size_t smem_bytes, cudaStream_t stream);
 // The difference-form mixed instances (flr_fused_d2.cu).
 const void *fused_fn_d2(bool grouped, bool diag, bool inner);
+// The difference-form mixed instances for sources that all start at t0 = +0
+// (flr_fused_t0.cu).
+const void *fused_fn_t0(bool grouped);
 // Serving instances (mixed; d2: difference forms for XYZ outputs): a launch
 // that claims published items until it is idle or stopped.  Sets the
 // instance's shared-memory limit before launching.

@@ -283,9 +283,13 @@ __device__ __forceinline__ df::f2 df_from_fixed(unsigned long long K, int fb) {
 // the significand m and fb = 52 - exponent): the same d and the same value of
 // eps, as a df, without FP64 conversions.  Other x take the FP64 route, the
 // ceiling as a round-up conversion ((double)(d + 1) equals 1.0 + d).
+// kT0Zero: t_first is +0 (every source of the launch starts at t0 = +0), and
+// delayed_t - (+0) is delayed_t for every double, so the subtraction is left
+// out: the same x with one FP64 operation fewer.
+template <bool kT0Zero = false>
 __device__ __forceinline__ void split_delay_df(double delayed_t, double t_first, double fs,
                                                int &d, df::f2 &eps) {
-    const double x = (delayed_t - t_first) * fs;
+    const double x = (kT0Zero ? delayed_t : delayed_t - t_first) * fs;
     const long long b = __double_as_longlong(x);
     const int e = (int)(b >> 52) - 1023;  // negative x: e < -1023
     if (e >= 0 && e <= 30) {
@@ -316,6 +320,25 @@ __device__ __forceinline__ double dot3_delay(const double *a, const double *b) {
     return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
 }
 
+// (double)j for a sample index (|j| < 2^52), assembled from the bits of j:
+// the exact value the conversion instruction gives, without that instruction
+// (conversions to FP64 take the FP64 pipe's issue slots).
+__device__ __forceinline__ double exact_double_of(long long j) {
+    const unsigned long long u = (unsigned long long)(j < 0 ? -j : j);
+    const int e = 63 - __clzll((long long)u);  // u = 0: -1 (replaced below)
+    const unsigned long long b = ((unsigned long long)(1023 + e) << 52) |
+                                 ((u << (52 - e)) & 0xfffffffffffffull) |
+                                 (j < 0 ? 0x8000000000000000ull : 0ull);
+    return __longlong_as_double(u == 0 ? 0ll : (long long)b);
+}
+
+// t0 + j dt, the reference's sample time; kT0Zero: t0 is +0 and j dt (never
+// -0) is the sum's exact value.
+template <bool kT0Zero>
+__device__ __forceinline__ double sample_time(double t0, long long j, double dt) {
+    return kT0Zero ? exact_double_of(j) * dt : t0 + exact_double_of(j) * dt;
+}
+
 struct MixedDelays {
     int d_rec, d_em;
     df::f2 e_rec, e_em;
@@ -325,6 +348,7 @@ struct MixedDelays {
 // Receiver/emitter delays exactly as link_geometry() computes them (same
 // operations, same order, so the integer indices are bit-identical), plus
 // the spacecraft positions for the projection factors.
+template <bool kT0Zero = false>
 __device__ __forceinline__ MixedDelays link_delays_mixed(const OrbitTables &o, double inv_dt,
                                                          int slot, double t, double t_first,
                                                          double fs, const double k[3]) {
@@ -336,8 +360,8 @@ __device__ __forceinline__ MixedDelays link_delays_mixed(const OrbitTables &o, d
     position_seg(o, orbit_segment_fast(o, inv_dt, t_em), t_em, o.sc_e[slot], g.x_em);
     double kx_rec = dot3_delay(k, g.x_rec);
     double kx_em = dot3_delay(k, g.x_em);
-    split_delay_df(t - kx_rec * kCInv, t_first, fs, g.d_rec, g.e_rec);
-    split_delay_df(t_em - kx_em * kCInv, t_first, fs, g.d_em, g.e_em);
+    split_delay_df<kT0Zero>(t - kx_rec * kCInv, t_first, fs, g.d_rec, g.e_rec);
+    split_delay_df<kT0Zero>(t_em - kx_em * kCInv, t_first, fs, g.d_em, g.e_em);
     return g;
 }
 
@@ -351,13 +375,14 @@ struct ReceiverSide {
     double x_rec[3];
 };
 
+template <bool kT0Zero = false>
 __device__ __forceinline__ ReceiverSide receiver_mixed(const OrbitTables &o, double inv_dt, int sc,
                                                        double t, double t_first, double fs,
                                                        const double k[3], const SegCache *sc_) {
     ReceiverSide r;
     r.w = seg_of(sc_, o, inv_dt, t);
     position_sb(o, r.w, t, sc, r.x_rec);
-    split_delay_df(t - dot3_delay(k, r.x_rec) * kCInv, t_first, fs, r.d_rec, r.e_rec);
+    split_delay_df<kT0Zero>(t - dot3_delay(k, r.x_rec) * kCInv, t_first, fs, r.d_rec, r.e_rec);
     return r;
 }
 
@@ -369,6 +394,7 @@ struct EmitterSide {
     double x_em[3];
 };
 
+template <bool kT0Zero = false>
 __device__ __forceinline__ EmitterSide emitter_mixed(const OrbitTables &o, double inv_dt, int slot,
                                                      Seg w, double t, double t_first, double fs,
                                                      const double k[3], const SegCache *sc_) {
@@ -377,7 +403,7 @@ __device__ __forceinline__ EmitterSide emitter_mixed(const OrbitTables &o, doubl
         (w.w < 0) ? 0.0 : orbit_lerp_b(o.ltt, o.ltt_slope, w.w, 6, slot, t, w.base);
     const double t_em = t - L;
     position_sb(o, seg_of(sc_, o, inv_dt, t_em), t_em, o.sc_e[slot], e.x_em);
-    split_delay_df(t_em - dot3_delay(k, e.x_em) * kCInv, t_first, fs, e.d_em, e.e_em);
+    split_delay_df<kT0Zero>(t_em - dot3_delay(k, e.x_em) * kCInv, t_first, fs, e.d_em, e.e_em);
     return e;
 }
 
@@ -1129,6 +1155,9 @@ __device__ __forceinline__ bool mixed_interp_any(const FusedArgs &a, const float
 // compiler's choice (a minimum of 0 blocks leaves it unspecified).
 // kInner: the instance that forms per-tile inner products with FusedSource
 // data (FusedArgs::partial) and writes the channels only where out is set.
+// kT0Zero: the instance for launches whose sources all start at t0 = +0: a
+// sample time t0 + j dt is then j dt and a split's t - t0 is t, bit for bit
+// (j dt is never -0), so the two FP64 operations are left out.
 // ------------------------------------------------ device-resident serving ----
 //
 // The server instances run the same item code over a source list that the
@@ -1202,9 +1231,11 @@ __device__ long long server_next_item(const FusedArgs &a, long long *slot, int t
     return w;
 }
 
-template <bool kMixed, bool kDiag, bool kGrouped, bool kInner, bool kD2, bool kServer = false>
+template <bool kMixed, bool kDiag, bool kGrouped, bool kInner, bool kD2, bool kServer = false,
+          bool kT0Zero = false>
 __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
     fused_kernel(const FusedArgs a) {
+    static_assert(!kT0Zero || (kMixed && !kServer), "the t0 = 0 instances are mixed batch instances");
     static_assert(!kServer || (kMixed && !kDiag && !kInner), "serving runs the plain mixed instances");
     static_assert(kMixed || !kD2, "the difference forms are mixed-arithmetic forms");
     static_assert(kMixed || !kGrouped, "the grouped form is a mixed-arithmetic form");
@@ -1371,10 +1402,10 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
             if (yfirst < ylast) {
                 const int slot = tid % 6;
                 const long j = (tid < 6) ? yfirst : ylast - 1;
-                const double t = t0 + (double)j * a.dt;
+                const double t = sample_time<kT0Zero>(t0, j, a.dt);
                 int dr, de;
                 if (kMixed) {
-                    MixedDelays g = link_delays_mixed(a.orb, a.inv_orbit_dt, slot, t, t0, a.fs, k);
+                    MixedDelays g = link_delays_mixed<kT0Zero>(a.orb, a.inv_orbit_dt, slot, t, t0, a.fs, k);
                     dr = g.d_rec;
                     de = g.d_em;
                 } else {
@@ -1521,17 +1552,17 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
                 const bool act = (sub < 10) && (jj < Y);
                 const long j = ya + jj;
                 const bool live = act && j >= yfirst && j < ylast;
-                const double t = t0 + (double)j * a.dt;
+                const double t = sample_time<kT0Zero>(t0, j, a.dt);
                 ReceiverSide rs{};
                 EmitterSide es{};
                 df::f2 re_r = {0.f, 0.f}, im_r = {0.f, 0.f}, re_e = {0.f, 0.f}, im_e = {0.f, 0.f};
                 df::f2 xr_df[3] = {}, xe_df[3] = {};  // positions for the projections
                 bool ok_r = false, ok_e = false;
                 if (live) {
-                    rs = receiver_mixed(a.orb, a.inv_orbit_dt, rr + 1, t, t0, a.fs, k, segc);
+                    rs = receiver_mixed<kT0Zero>(a.orb, a.inv_orbit_dt, rr + 1, t, t0, a.fs, k, segc);
                     ok_r = mixed_interp_any<kD2>(a, hdf, dh, wlo, W, hsrc, scale, n, rs.d_rec,
                                             rs.e_rec, inv_deps_df, edf, h, re_r, im_r);
-                    es = emitter_mixed(a.orb, a.inv_orbit_dt, a.tx_slot[rr], rs.w, t, t0, a.fs, k,
+                    es = emitter_mixed<kT0Zero>(a.orb, a.inv_orbit_dt, a.tx_slot[rr], rs.w, t, t0, a.fs, k,
                                        segc);
                     ok_e = mixed_interp_any<kD2>(a, hdf, dh, wlo, W, hsrc, scale, n, es.d_em,
                                             es.e_em, inv_deps_df, edf, h, re_e, im_e);
@@ -1590,17 +1621,17 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
                     y32[a.rx_slot[r][1] * a.y_max + jj] = make_float2(0.f, 0.f);
                     continue;
                 }
-                const double t = t0 + (double)j * a.dt;
+                const double t = sample_time<kT0Zero>(t0, j, a.dt);
                 const bool own = (j >= o0 && j < o1);  // this tile's outputs: diagnostics
                 const ReceiverSide rs =
-                    receiver_mixed(a.orb, a.inv_orbit_dt, a.rx_sc[r], t, t0, a.fs, k, segc);
+                    receiver_mixed<kT0Zero>(a.orb, a.inv_orbit_dt, a.rx_sc[r], t, t0, a.fs, k, segc);
                 df::f2 re_r, im_r;
                 const bool ok_r = mixed_interp_any<kD2>(a, hdf, dh, wlo, W, hsrc, scale, n, rs.d_rec,
                                                    rs.e_rec, inv_deps_df, edf, h, re_r, im_r);
                 for (int q = 0; q < 2; ++q) {
                     const int slot = a.rx_slot[r][q];
                     const EmitterSide es =
-                        emitter_mixed(a.orb, a.inv_orbit_dt, slot, rs.w, t, t0, a.fs, k, segc);
+                        emitter_mixed<kT0Zero>(a.orb, a.inv_orbit_dt, slot, rs.w, t, t0, a.fs, k, segc);
                     if (kDiag && own && src.d_rec_out) {
                         src.d_rec_out[(long)slot * n + j] = rs.d_rec;
                         src.d_em_out[(long)slot * n + j] = es.d_em;
@@ -1637,7 +1668,7 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
                 const bool act = (sub < 10) && (jj < Y);
                 const long j = ya + jj;
                 const bool live = act && j >= yfirst && j < ylast;
-                const double t = t0 + (double)j * a.dt;
+                const double t = sample_time<kT0Zero>(t0, j, a.dt);
                 ReceiverF64 rs{};
                 double x_em[3] = {0.0, 0.0, 0.0};
                 int d_em = 0;
@@ -1708,7 +1739,7 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
                     y64[a.rx_slot[r][1] * a.y_max + jj] = 0.0;
                     continue;
                 }
-                const double t = t0 + (double)j * a.dt;
+                const double t = sample_time<kT0Zero>(t0, j, a.dt);
                 const bool own = (j >= o0 && j < o1);
                 const ReceiverF64 rs = receiver_f64(a.orb, a.rx_sc[r], t, t0, a.fs, k);
                 double A_r, hp_r = 0.0, hc_r = 0.0;
@@ -1756,9 +1787,9 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
                     y64[slot * a.y_max + jj] = 0.0;
                 continue;
             }
-            const double t = t0 + (double)j * a.dt;
+            const double t = sample_time<kT0Zero>(t0, j, a.dt);
             if (kMixed) {
-                const MixedDelays g = link_delays_mixed(a.orb, a.inv_orbit_dt, slot, t, t0, a.fs, k);
+                const MixedDelays g = link_delays_mixed<kT0Zero>(a.orb, a.inv_orbit_dt, slot, t, t0, a.fs, k);
                 const bool own = (j >= o0 && j < o1);  // this tile's outputs: diagnostics
                 if (kDiag && own && src.d_rec_out) {
                     src.d_rec_out[(long)slot * n + j] = g.d_rec;
@@ -1907,7 +1938,7 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
         double lk[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // inner products (kInner)
         if (kGrouped) {
             for (long i = o0 + tid; i < o1; i += kThreads) {
-                const double t = t0 + (double)i * a.dt;
+                const double t = sample_time<kT0Zero>(t0, i, a.dt);
                 const Seg w = seg_of(segc, a.orb, a.inv_orbit_dt, t);
                 // every link has this L(t): the delay of a list of length m is t - L - ... - L
                 const double L0 =
@@ -1922,7 +1953,7 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
                         delay = delay - L0;
                     int d;
                     df::f2 e_df;
-                    split_delay_df(delay, t0, a.fs, d, e_df);
+                    split_delay_df<kT0Zero>(delay, t0, a.fs, d, e_df);
                     if (kDiag && src.d_tdi_out)
                         for (int u = set->group_start[g]; u < set->group_start[g + 1]; ++u)
                             src.d_tdi_out[(long)set->orig_unit[u] * n + i] = d;
@@ -1984,7 +2015,7 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
             }
         } else {
             for (long i = o0 + tid; i < o1; i += kThreads) {
-                const double t = t0 + (double)i * a.dt;
+                const double t = sample_time<kT0Zero>(t0, i, a.dt);
                 double L[kLinks];
                 if (kMixed) {
                     const Seg w = seg_of(segc, a.orb, a.inv_orbit_dt, t);
@@ -2017,7 +2048,7 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
                         // consecutive units with bit-identical delays share the split
                         const long long bits = __double_as_longlong(delay);
                         if (bits != prev_bits) {
-                            split_delay_df(delay, t0, a.fs, d, e_df);
+                            split_delay_df<kT0Zero>(delay, t0, a.fs, d, e_df);
                             if (kD2)
                                 w2 = d2_weights(a, inv_deps_df, e_df);
                             else

@@ -36,6 +36,7 @@ SOURCES = {
     "flr_fused.cu": ["--fmad=false"],
     "flr_fused_d2.cu": ["--fmad=false"],
     "flr_fused_server.cu": ["--fmad=false"],
+    "flr_fused_t0.cu": ["--fmad=false"],
     "flr_batch.cu": [],
     "flr_waveform.cu": ["--fmad=false"],
 }

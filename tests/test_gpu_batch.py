@@ -210,3 +210,32 @@ def test_batch_mixed_bits_do_not_depend_on_the_tile(gpu_lib, orbit_kind):
     for tile in (128, 1024):
         for a, b in zip(outs[tile], outs[512]):
             assert np.array_equal(a, b), f"tile {tile}"
+
+
+@pytest.mark.parametrize("orbit_kind", ["equal", "kepler"])
+def test_t0_zero_instance_matches_general(gpu_lib, orbit_kind):
+    """Sources that all start at t0 = +0 take the fused kernel's instance
+    without the t0 operations; the same sources beside one with t0 != 0 (or
+    with t0 = -0) take the general instance: the same bits, in direct runs and
+    in graph replays."""
+    import fastlisaresponse_gb300 as flr
+
+    dt = 10.0
+    orb = flr.EqualArmlengthOrbits(t_max=1.2e6) if orbit_kind == "equal" else \
+        flr.KeplerianOrbits(t_max=1.2e6)
+    bat = flr.BatchedResponseTDI(1 / dt, order=25, tdi=["1st generation", "2nd generation"],
+                                 orbits=orb, precision="mixed")
+    hs, lam, beta, _ = _sources(orb, dt, [2500, 9000, 40000, 70001, 30000], seed=11)
+    sets = [0, 1, 1, 0, 1]
+    zero = np.zeros(4)
+    alone = [_np(o) for o in bat(hs[:4], lam[:4], beta[:4], t0=zero, tdi_set=sets[:4])]
+    beside = bat(hs, lam, beta, t0=np.append(zero, 5e3), tdi_set=sets)
+    negzero = bat(hs[:4], lam[:4], beta[:4], t0=np.full(4, -0.0), tdi_set=sets[:4])
+    for a, b, c in zip(alone, beside, negzero):
+        assert np.array_equal(a, _np(b)) and np.array_equal(a, _np(c))
+    g = bat.graph(8)
+    via_graph = g(hs[:4], lam[:4], beta[:4], t0=zero, tdi_set=sets[:4])
+    via_graph_beside = g(hs, lam, beta, t0=np.append(zero, 5e3), tdi_set=sets)
+    for a, b, c in zip(alone, via_graph, via_graph_beside):
+        assert np.array_equal(a, _np(b)) and np.array_equal(a, _np(c))
+    assert bat.status() == 0
