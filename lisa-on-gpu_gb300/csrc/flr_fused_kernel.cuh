@@ -1441,7 +1441,7 @@ __global__ void __launch_bounds__(kThreads, (kMixed && !kDiag) ? 3 : 0)
         if (W > 0 && src.h == nullptr) {
             const GbCoefs gc = gb_coefs(*gbp);
             for (int i = tid; i < W; i += kThreads)
-                hraw[i] = gb_sample(gc, t0 + (double)(wlo + i) * a.dt);
+                hraw[i] = gb_sample(gc, t0 + exact_double_of(wlo + i) * a.dt);
             __syncthreads();
         } else if (W > 0) {
             if (tid == 0) {
