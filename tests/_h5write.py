@@ -10,10 +10,11 @@ two styles the HDF5 library writes, for the reader in
   lookup3 checksums, groups as link messages -- h5py with
   ``libver="latest"``, continuation blocks ("OCHK") likewise.
 
-Datasets are contiguous, or chunked with a version-1 B-tree chunk index (two
-levels beyond four chunks) and the shuffle + deflate filters.  Attributes: float64 / int64 scalars and
-arrays, variable-length UTF-8 strings (global heap).  Only what the tests
-need; no free-space management.
+Datasets are contiguous, chunked with a version-1 B-tree chunk index (two
+levels beyond four chunks) and the shuffle + deflate filters, or compact
+(the data inside the layout message).  Attributes: numeric scalars and
+arrays, fixed-length strings, variable-length UTF-8 strings (global heap).
+Only what the tests need; no free-space management.
 """
 
 from __future__ import annotations
@@ -84,6 +85,8 @@ def _dtype_msg(dt: np.dtype) -> bytes:
     if dt.kind in "iu":
         bits = order | (0x08 if dt.kind == "i" else 0)
         return bytes([0x10, bits, 0, 0]) + _u(dt.itemsize, 4) + _u(0, 2) + _u(dt.itemsize * 8, 2)
+    if dt.kind == "S":  # fixed-length, null-padded ASCII
+        return bytes([0x13, 0x01, 0, 0]) + _u(dt.itemsize, 4)
     raise TypeError(dt)
 
 
@@ -114,10 +117,10 @@ class Writer:
             node = node["members"].setdefault(part, {"attrs": {}, "members": {}})
         return node
 
-    def dataset(self, path: str, data, chunks=None, attrs=None) -> None:
+    def dataset(self, path: str, data, chunks=None, attrs=None, compact=False) -> None:
         parent, _, name = path.rpartition("/")
         self.group(parent)["members"][name] = {"data": np.asarray(data), "chunks": chunks,
-                                               "attrs": dict(attrs or {})}
+                                               "attrs": dict(attrs or {}), "compact": compact}
 
     # -- file space ---------------------------------------------------------------------
     def alloc(self, data: bytes) -> int:
@@ -182,7 +185,9 @@ class Writer:
         data, chunks = node["data"], node["chunks"]
         v2 = self.style == "v2"
         msgs = [(0x03, _dtype_msg(data.dtype)), (0x01, _space_msg(data.shape, v2))]
-        if chunks is None:
+        if node.get("compact"):  # the raw data inside the layout message
+            msgs.append((0x08, bytes([3, 0]) + _u(data.nbytes, 2) + data.tobytes()))
+        elif chunks is None:
             a = self.alloc(data.tobytes())
             msgs.append((0x08, bytes([3, 1]) + _u(a, 8) + _u(data.nbytes, 8)))
         else:

@@ -172,3 +172,41 @@ def test_writer_checksum_known_answers():
     assert lookup3(b"") == 0xDEADBEEF
     assert lookup3(b"Four score and seven years ago") == 0x17770551
     assert lookup3(b"Four score and seven years ago", 1) == 0xCD628161
+
+
+@pytest.mark.parametrize("style", ["v0", "v2"])
+def test_h5lite_dataset_forms(tmp_path, style):
+    """Compact and scalar datasets, integers of every width and byte order,
+    fixed-length strings, and attribute arrays."""
+    from _h5write import Writer
+
+    from fastlisaresponse_gb300 import h5lite
+
+    rng = np.random.default_rng(4)
+    w = Writer(style)
+    forms = {
+        "i1": rng.integers(-100, 100, 7).astype("i1"),
+        "u2be": rng.integers(0, 60000, (3, 4)).astype(">u2"),
+        "i4": rng.integers(-2**30, 2**30, 9).astype("<i4"),
+        "u8": rng.integers(0, 2**62, 5).astype("<u8"),
+        "f4be": rng.normal(size=6).astype(">f4"),
+        "scalar": np.array(2.5),
+        "names": np.array([b"tcb", b"tps", b"x"], dtype="S4"),
+    }
+    for name, arr in forms.items():
+        w.dataset(f"forms/{name}", arr, compact=name in ("i1", "scalar", "names"))
+    w.dataset("forms/chunked_i4", forms["i4"], chunks=(4,))
+    w.root["attrs"].update({"label": np.array(b"LISA", dtype="S8"), "ints": np.arange(4),
+                            "dt": 10.0})
+    path = tmp_path / f"forms_{style}.h5"
+    w.save(path)
+    with h5lite.File(path) as f:
+        for name, arr in forms.items():
+            ds = f["forms"][name]
+            got = ds[()]
+            assert ds.shape == arr.shape
+            assert np.array_equal(got, arr) and got.dtype == arr.dtype.newbyteorder("=")
+        assert np.array_equal(f["forms/chunked_i4"][()], forms["i4"])
+        assert f.attrs["label"] == b"LISA" and np.array_equal(f.attrs["ints"], np.arange(4))
+        assert sorted(f["forms"].keys()) == sorted(list(forms) + ["chunked_i4"])
+        assert len(f["forms"]) == len(forms) + 1 and "dt" in f.attrs
