@@ -143,6 +143,18 @@ struct SharedC128 {
     __device__ __forceinline__ double2 operator[](long i) const { return p[i]; }
 };
 
+// (double)j for an integer |j| < 2^52, assembled from the bits of j: the
+// exact value the conversion instruction gives, without that instruction
+// (conversions to FP64 take the FP64 pipe's issue slots).
+__device__ __forceinline__ double exact_double_of(long long j) {
+    const unsigned long long u = (unsigned long long)(j < 0 ? -j : j);
+    const int e = 63 - __clzll((long long)u);  // u = 0: -1 (replaced below)
+    const unsigned long long b = ((unsigned long long)(1023 + e) << 52) |
+                                 ((u << (52 - e)) & 0xfffffffffffffull) |
+                                 (j < 0 ? 0x8000000000000000ull : 0ull);
+    return __longlong_as_double(u == 0 ? 0ll : (long long)b);
+}
+
 // Real 2h-point Lagrange interpolation of x around sample d (interp_single,
 // LISAResponse.cu:110-147).  The caller guarantees d-h+1 >= 0 and d+h < n.
 template <class Src>
@@ -151,8 +163,9 @@ __device__ __forceinline__ double lagrange_real(const Src &x, int d, double eps,
     double w_up = 1.0 - eps, w_dn = eps, w_tail = eps * (1.0 - eps);
     double tail = 0.0;
     for (int j = 1; j < lt.h; ++j) {
-        double f = (double)j + eps;
-        double g = (double)j + (1.0 - eps);
+        const double jd = exact_double_of(j);
+        double f = jd + eps;
+        double g = jd + (1.0 - eps);
         double up = x[d + 1 + j];
         double dn = x[d - j];
         tail += __ldg(lt.E + j - 1) * (up / f + dn / g);
@@ -168,8 +181,9 @@ __device__ __forceinline__ void lagrange_c128(const Src &x, int d, double eps, d
     double w_up = 1.0 - eps, w_dn = eps, w_tail = eps * (1.0 - eps);
     double tail_re = 0.0, tail_im = 0.0;
     for (int j = 1; j < lt.h; ++j) {
-        double f = (double)j + eps;
-        double g = (double)j + (1.0 - eps);
+        const double jd = exact_double_of(j);
+        double f = jd + eps;
+        double g = jd + (1.0 - eps);
         double2 up = x[d + 1 + j];
         double2 dn = x[d - j];
         double e = __ldg(lt.E + j - 1);

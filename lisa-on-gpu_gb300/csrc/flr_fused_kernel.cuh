@@ -320,18 +320,6 @@ __device__ __forceinline__ double dot3_delay(const double *a, const double *b) {
     return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
 }
 
-// (double)j for a sample index (|j| < 2^52), assembled from the bits of j:
-// the exact value the conversion instruction gives, without that instruction
-// (conversions to FP64 take the FP64 pipe's issue slots).
-__device__ __forceinline__ double exact_double_of(long long j) {
-    const unsigned long long u = (unsigned long long)(j < 0 ? -j : j);
-    const int e = 63 - __clzll((long long)u);  // u = 0: -1 (replaced below)
-    const unsigned long long b = ((unsigned long long)(1023 + e) << 52) |
-                                 ((u << (52 - e)) & 0xfffffffffffffull) |
-                                 (j < 0 ? 0x8000000000000000ull : 0ull);
-    return __longlong_as_double(u == 0 ? 0ll : (long long)b);
-}
-
 // t0 + j dt, the reference's sample time; kT0Zero: t0 is +0 and j dt (never
 // -0) is the sum's exact value.
 template <bool kT0Zero>
