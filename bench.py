@@ -487,7 +487,10 @@ def run_headline(args, device, peaks, rank, world):
                       f"(perfmodel.mixed_index_ops_grouped: {idx_ops['total']}) x output "
                       "samples / one launch's CUDA-event time; the double-float taps run on "
                       "the FP32 pipe, not counted; peak = FP64 FMA probe of this run "
-                      "(MEASURED_PEAKS.json has no FP64 figure)",
+                      "(MEASURED_PEAKS.json has no FP64 figure); the count is the reference "
+                      "formula's, part of which the kernel does as integer work (index "
+                      "splits and sample times from the bits, no t0 operations at t0 = 0), "
+                      "so the fraction can reach 1 below FP64-pipe saturation",
         "launch_ms": 1e3 * launch_secs,
         "traffic": (traffic["bytes_per_output_sample"] * n_out) if traffic else None,
         "traffic_source": traffic["source"] if traffic else None,
